@@ -1,0 +1,231 @@
+"""Seeded synthetic inputs: water clusters, an anatase TiO2 sphere, and analytic SK tables.
+
+The reference measures on nothing public for this path, so every workload is generated here from a
+seed (``numpy.random.Generator(PCG64)``):
+
+* Water: O at uniform positions in a sphere with min O-O 2.6 A, uniform random orientation
+  (normalised Gaussian quaternion), O-H 0.96 A, H-O-H 104.5 deg. Atom order per molecule O, H, H.
+* SK tables on a 0.02 Bohr grid with 600 rows (r = 0.02 ... 12.00 Bohr; cutoff 13 Bohr):
+  H integral = -A exp(-a r)(1 + b r), S integral = B exp(-c r)(1 + d r + e r^2), with
+  A in [0.2, 0.6] Ha, a in [0.5, 1.2], B in [0.3, 0.9], c in [0.4, 1.0], b, d, e in [0, 0.3],
+  drawn per (species pair, integral). A draw whose overlap is not safely positive definite on the
+  target geometries is rejected and the next draw index is used (``rng = default_rng([seed, k])``).
+* Pair repulsive: K exp(-beta r) minus its 2nd-order Taylor polynomial at rc = 4 Bohr, written as
+  the SKF ``Spline`` block (exponential head below 1.0 Bohr, 0.1 Bohr cubic segments, 5th-order
+  last segment); K in [0.5, 2.0] Ha, beta in [1.0, 2.0] / Bohr.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from .model import Model, PairTable, Species
+from .skf import SkfData, SplineRepulsive, full_table
+
+BOHR_AA = 0.529177249          # Bohr in Angstrom (common/constants.F90:28)
+AA_BOHR = 1.0 / BOHR_AA
+
+GRID_DIST = 0.02               # Bohr
+GRID_ROWS = 600                # rows r = dist .. rows*dist
+REP_CUTOFF = 4.0               # Bohr
+
+# Species definitions (on-site energies, U and valence occupations per shell)
+SPECIES_O = Species("O", [0, 1], [-0.87, -0.33], 0.50, [2.0, 4.0], 16.0)
+SPECIES_H = Species("H", [0], [-0.24], 0.42, [1.0], 1.008)
+SPECIES_TI = Species("Ti", [0, 1, 2], [-0.17, -0.06, -0.20], 0.32, [2.0, 0.0, 2.0], 47.87)
+
+# Draw index accepted by the table search in oracle/select_tables.py (lambda_min(S) >= 0.2 on the
+# water workloads and a HOMO-LUMO gap well above kT); tests re-verify it.
+WATER_SEED = 20261204
+WATER_DRAW = 4
+
+
+# ---------------------------------------------------------------------------------------- tables
+def _draw_h(rng):
+    A = rng.uniform(0.2, 0.6)
+    a = rng.uniform(0.5, 1.2)
+    b = rng.uniform(0.0, 0.3)
+    return A, a, b
+
+
+def _draw_s(rng):
+    B = rng.uniform(0.3, 0.9)
+    c = rng.uniform(0.4, 1.0)
+    d = rng.uniform(0.0, 0.3)
+    e = rng.uniform(0.0, 0.3)
+    return B, c, d, e
+
+
+def _h_fun(p, r):
+    A, a, b = p
+    return -A * np.exp(-a * r) * (1.0 + b * r)
+
+
+def _s_fun(p, r):
+    B, c, d, e = p
+    return B * np.exp(-c * r) * (1.0 + d * r + e * r * r)
+
+
+# File column index (10-column format dd0 dd1 dd2 pd0 pd1 pp0 pp1 sd0 sp0 ss0) of (lmin, lmax, m)
+_COL10 = {(2, 2, 0): 0, (2, 2, 1): 1, (2, 2, 2): 2, (1, 2, 0): 3, (1, 2, 1): 4,
+          (1, 1, 0): 5, (1, 1, 1): 6, (0, 2, 0): 7, (0, 1, 0): 8, (0, 0, 0): 9}
+
+
+def _repulsive(K: float, beta: float, rc: float = REP_CUTOFF, r0: float = 1.0,
+               seg: float = 0.1) -> SplineRepulsive:
+    """Piecewise-polynomial form of g(r) = K e^{-beta r} - T2(r), T2 = Taylor(2) of K e^{-beta r} at rc."""
+    e_rc = K * math.exp(-beta * rc)
+
+    def deriv(r, k):  # k-th derivative of g
+        val = K * (-beta) ** k * math.exp(-beta * r)
+        dr = r - rc
+        if k == 0:
+            val -= e_rc * (1.0 - beta * dr + 0.5 * beta * beta * dr * dr)
+        elif k == 1:
+            val -= e_rc * (-beta + beta * beta * dr)
+        elif k == 2:
+            val -= e_rc * beta * beta
+        return val
+
+    n_spl = int(round((rc - r0) / seg))
+    xs = r0 + seg * np.arange(n_spl)
+    cub = np.array([[deriv(x, 0), deriv(x, 1), deriv(x, 2) / 2.0, deriv(x, 3) / 6.0] for x in xs[:-1]])
+    xl = xs[-1]
+    last = np.array([deriv(xl, k) / math.factorial(k) for k in range(6)])
+    g0, g1 = deriv(r0, 0), deriv(r0, 1)
+    a1 = -g1 / g0
+    a2 = math.log(g0) + a1 * r0
+    return SplineRepulsive(cutoff=rc, exp_coeffs=np.array([a1, a2, 0.0]), x_start=xs,
+                           sp_coeffs=cub, last_coeffs=last)
+
+
+def make_skf_set(species: Sequence[Species], seed: int, draw: int) -> Dict[Tuple[int, int], SkfData]:
+    """Analytic SK tables for all ordered species pairs; ``draw`` selects the sub-stream."""
+    rng = np.random.default_rng([seed, draw])
+    ns = len(species)
+    r = GRID_DIST * np.arange(1, GRID_ROWS + 1)
+    files: Dict[Tuple[int, int], Tuple[np.ndarray, np.ndarray]] = {}
+    for a in range(ns):
+        for b in range(ns):
+            files[(a, b)] = (np.zeros((GRID_ROWS, 10)), np.zeros((GRID_ROWS, 10)))
+    reps = {}
+    for a in range(ns):
+        for b in range(a, ns):
+            la_set, lb_set = species[a].shells, species[b].shells
+            # integrals <a, l1 | b, l2> with l1 <= l2 live in file a-b; with l1 > l2 in file b-a
+            todo = []
+            for l1 in la_set:
+                for l2 in lb_set:
+                    if a == b and l1 > l2:
+                        continue
+                    todo.append((l1, l2))
+            for (l1, l2) in todo:
+                for m in range(min(l1, l2) + 1):
+                    ph, ps = _draw_h(rng), _draw_s(rng)
+                    hv, sv = _h_fun(ph, r), _s_fun(ps, r)
+                    if l1 <= l2:
+                        col = _COL10[(l1, l2, m)]
+                        files[(a, b)][0][:, col] = hv
+                        files[(a, b)][1][:, col] = sv
+                        if l1 == l2 and a != b:
+                            files[(b, a)][0][:, col] = hv
+                            files[(b, a)][1][:, col] = sv
+                    else:
+                        col = _COL10[(l2, l1, m)]
+                        files[(b, a)][0][:, col] = hv
+                        files[(b, a)][1][:, col] = sv
+            K = rng.uniform(0.5, 2.0)
+            beta = rng.uniform(1.0, 2.0)
+            reps[(a, b)] = reps[(b, a)] = _repulsive(K, beta)
+    out = {}
+    for (a, b), (h10, s10) in files.items():
+        ham = np.zeros((GRID_ROWS, 20))
+        over = np.zeros((GRID_ROWS, 20))
+        from .skf import OLD_SLOTS
+        for k, slot in enumerate(OLD_SLOTS):
+            ham[:, slot - 1] = h10[:, k]
+            over[:, slot - 1] = s10[:, k]
+        sp = species[a]
+        homo = a == b
+        ons = np.zeros(3); hub = np.zeros(3); occ = np.zeros(3)
+        if homo:
+            for l, e_, o_ in zip(sp.shells, sp.onsite, sp.occ):
+                ons[l] = e_; occ[l] = o_
+            hub[:] = sp.hubbu
+        out[(a, b)] = SkfData(dist=GRID_DIST, ham=ham, over=over,
+                              onsite=ons if homo else None, hubbu=hub if homo else None,
+                              occ=occ if homo else None, mass=sp.mass if homo else None,
+                              repulsive=reps[(a, b)])
+    return out
+
+
+def skf_columns10(d: SkfData) -> Tuple[np.ndarray, np.ndarray]:
+    from .skf import OLD_SLOTS
+    idx = [s - 1 for s in OLD_SLOTS]
+    return d.ham[:, idx], d.over[:, idx]
+
+
+def water_model(seed: int = WATER_SEED, draw: int = WATER_DRAW) -> Model:
+    species = [SPECIES_O, SPECIES_H]
+    return Model.from_skf(species, make_skf_set(species, seed, draw))
+
+
+def tio2_model(seed: int = WATER_SEED + 1, draw: int = 0) -> Model:
+    species = [SPECIES_TI, SPECIES_O]
+    return Model.from_skf(species, make_skf_set(species, seed, draw))
+
+
+# ---------------------------------------------------------------------------------------- geometry
+def _rotation_from_quaternion(q):
+    w, x, y, z = q / np.linalg.norm(q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def water_cluster(n_mol: int, radius_aa: float, seed: int, min_oo_aa: float = 2.6,
+                  max_tries: int = 10_000_000):
+    """(coords[3, N] in Bohr, species[N] with O=0, H=1) for a seeded (H2O)n cluster."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    oxy = np.zeros((0, 3))
+    tries = 0
+    while oxy.shape[0] < n_mol:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("could not place water molecules")
+        p = rng.uniform(-radius_aa, radius_aa, 3)
+        if p @ p > radius_aa * radius_aa:
+            continue
+        if oxy.shape[0] and np.min(np.sum((oxy - p) ** 2, axis=1)) < min_oo_aa ** 2:
+            continue
+        oxy = np.vstack([oxy, p])
+    half = math.radians(104.5) / 2.0
+    roh = 0.96
+    h_local = np.array([[roh * math.sin(half), 0.0, roh * math.cos(half)],
+                        [-roh * math.sin(half), 0.0, roh * math.cos(half)]])
+    coords = []
+    for i in range(n_mol):
+        rot = _rotation_from_quaternion(rng.normal(size=4))
+        o = oxy[i]
+        coords.append(o)
+        for h in h_local:
+            coords.append(o + rot @ h)
+    coords = np.array(coords).T * AA_BOHR
+    species = np.tile(np.array([0, 1, 1], dtype=np.int32), n_mol)
+    return np.ascontiguousarray(coords), species
+
+
+def batched_water_sizes(n_systems: int, seed: int, lo: int = 2, hi: int = 48) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.integers(lo, hi + 1, size=n_systems)
+
+
+def batched_water(n_systems: int, seed: int):
+    """List of (coords, species) for the ragged batch: n ~ U[2, 48], radius 10 A (n/32)^(1/3)."""
+    sizes = batched_water_sizes(n_systems, seed)
+    out = []
+    for i, n in enumerate(sizes):
+        out.append(water_cluster(int(n), 10.0 * (n / 32.0) ** (1.0 / 3.0), seed * 7919 + i))
+    return out
