@@ -1,0 +1,249 @@
+"""ctypes binding of libdftbgpu.so (C-ABI in include/dftbgpu.h) and the user-facing calculator.
+
+``DftbGpu`` mirrors the reference's Python API (tools/pythonapi/src/dftbplus/dftbplus.py:25-399,
+class ``DftbPlus``): ``set_geometry``, ``get_nr_atoms``, ``get_energy`` (Mermin free energy),
+``get_gradients`` (gradients, not forces) and ``get_gross_charges`` (q0 - q per atom), with the
+same units (Bohr, Hartree) and the same error behaviour (an exception on failure). There is no CPU
+path: without the CUDA library or a GPU, construction fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .model import Model
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdftbgpu.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "overlap not positive definite",
+          4: "SCC not converged", 5: "Fermi level search failed", 6: "iteration cap reached",
+          7: "invalid call order", 8: "no CUDA device"}
+
+
+class SccOpts(C.Structure):
+    _fields_ = [("kT", C.c_double), ("scc_tol", C.c_double), ("max_iter", C.c_int), ("min_iter", C.c_int),
+                ("mix_alpha", C.c_double), ("mix_omega0", C.c_double), ("mix_min_weight", C.c_double),
+                ("mix_max_weight", C.c_double), ("mix_weight_fac", C.c_double), ("net_charge", C.c_double),
+                ("precision", C.c_int), ("convergent_only", C.c_int)]
+
+
+class Energies(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("EnonSCC", "Escc", "Erep", "Eband", "TS", "E0", "Etotal", "EMermin")]
+
+    def as_dict(self) -> dict:
+        return {k: float(getattr(self, k)) for k, _ in self._fields_}
+
+
+# name -> (restype, argtypes); every entry point declared in include/dftbgpu.h
+SIGNATURES = {
+    "dftbgpu_default_opts": (None, [C.POINTER(SccOpts)]),
+    "dftbgpu_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "dftbgpu_destroy": (C.c_int, [C.c_void_p]),
+    "dftbgpu_last_error": (C.c_char_p, [C.c_void_p]),
+    "dftbgpu_set_model": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _dp, _ip, _dp]),
+    "dftbgpu_set_geometry": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip]),
+    "dftbgpu_set_geometry_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, _ip]),
+    "dftbgpu_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), _dp, C.POINTER(Energies), _dp, _dp, _dp, _dp, _ip, _ip]),
+    "dftbgpu_gradients": (C.c_int, [C.c_void_p, _dp]),
+    "dftbgpu_gradients_dev": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dftbgpu_n_orbitals": (C.c_int, [C.c_void_p, _ip]),
+    "dftbgpu_get_orbital_populations": (C.c_int, [C.c_void_p, _dp]),
+    "dftbgpu_sygvd": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
+    "dftbgpu_get_matrix": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "dftbgpu_kernel_launches": (C.c_longlong, [C.c_void_p]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libdftbgpu.so (raises if it is missing: there is no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} not found: build it with dftbplus_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class DftbGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dftbgpu error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Context:
+    """Thin owner of a dftbgpu_ctx handle."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.dftbgpu_create(C.byref(h), device)
+        if rc != 0:
+            raise DftbGpuError(rc, "dftbgpu_create failed")
+        self.h = h
+
+    def check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.dftbgpu_last_error(self.h)
+            raise DftbGpuError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dftbgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_model(self, model: Model):
+        p = model.pack()
+        self._model_arrays = p  # keep alive
+        a = {k: np.ascontiguousarray(v) for k, v in p.items() if isinstance(v, np.ndarray)}
+        self.check(self.lib.dftbgpu_set_model(
+            self.h, p["n_species"], _p(a["n_shell"], C.c_int), _p(a["ang_shell"], C.c_int),
+            _p(a["onsite"], C.c_double), _p(a["hubbu"], C.c_double), _p(a["ref_occ"], C.c_double),
+            _p(a["sk_dist"], C.c_double), _p(a["sk_rows"], C.c_int), _p(a["sk_nint"], C.c_int),
+            _p(a["sk_ham"], C.c_double), _p(a["sk_over"], C.c_double), _p(a["rep_nspline"], C.c_int),
+            _p(a["rep_data"], C.c_double)))
+
+    def set_geometry(self, coords: np.ndarray, species: np.ndarray):
+        xyz = np.ascontiguousarray(np.asarray(coords, dtype=np.float64).T)  # (N, 3): x,y,z per atom
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        self.check(self.lib.dftbgpu_set_geometry(self.h, len(sp), _p(xyz, C.c_double), _p(sp, C.c_int)))
+        self.natom = len(sp)
+        n = C.c_int()
+        self.check(self.lib.dftbgpu_n_orbitals(self.h, C.byref(n)))
+        self.norb = n.value
+
+    def scc(self, opts: SccOpts, q_init: Optional[np.ndarray] = None):
+        en = Energies()
+        ef = C.c_double()
+        eig = np.zeros(self.norb)
+        fill = np.zeros(self.norb)
+        qout = np.zeros(self.natom)
+        nit = C.c_int()
+        conv = C.c_int()
+        qi = None
+        if q_init is not None:
+            qi = np.ascontiguousarray(q_init, dtype=np.float64)
+        self.check(self.lib.dftbgpu_scc(self.h, C.byref(opts), _p(qi, C.c_double) if qi is not None else None,
+                                        C.byref(en), C.byref(ef), _p(eig, C.c_double), _p(fill, C.c_double),
+                                        _p(qout, C.c_double), C.byref(nit), C.byref(conv)))
+        return dict(energies=en.as_dict(), ef=ef.value, eig=eig, filling=fill, q_out=qout, n_iter=nit.value,
+                    converged=bool(conv.value))
+
+    def gradients(self) -> np.ndarray:
+        g = np.zeros(3 * self.natom)
+        self.check(self.lib.dftbgpu_gradients(self.h, _p(g, C.c_double)))
+        return g.reshape(self.natom, 3).T.copy()
+
+    def orbital_populations(self) -> np.ndarray:
+        q = np.zeros(self.norb)
+        self.check(self.lib.dftbgpu_get_orbital_populations(self.h, _p(q, C.c_double)))
+        return q
+
+    def matrix(self, which: int) -> np.ndarray:
+        out = np.zeros((self.norb, self.norb), order="F")
+        self.check(self.lib.dftbgpu_get_matrix(self.h, which, _p(out, C.c_double)))
+        return out
+
+    def sygvd(self, a: np.ndarray, b: np.ndarray):
+        n = a.shape[0]
+        A = np.asfortranarray(a, dtype=np.float64).copy(order="F")
+        B = np.asfortranarray(b, dtype=np.float64).copy(order="F")
+        w = np.zeros(n)
+        self.check(self.lib.dftbgpu_sygvd(self.h, n, _p(A, C.c_double), _p(B, C.c_double), _p(w, C.c_double)))
+        return w, A, B
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.dftbgpu_kernel_launches(self.h))
+
+
+def default_opts(**kw) -> SccOpts:
+    o = SccOpts()
+    load_library().dftbgpu_default_opts(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class DftbGpu:
+    """SCC-DFTB calculator on one GB300, API-compatible with the reference's ``DftbPlus`` for
+    the non-periodic energy/gradient/charge queries."""
+
+    def __init__(self, model: Model, coords: np.ndarray, species: np.ndarray, kT: float = 1e-3,
+                 scc_tol: float = 1e-7, max_iter: int = 100, mixing: float = 0.2, device: int = 0,
+                 precision: int = PREC_FP64):
+        self.ctx = Context(device)
+        self.ctx.set_model(model)
+        self.model = model
+        self.species = np.asarray(species, dtype=np.int32)
+        self.opts = default_opts(kT=kT, scc_tol=scc_tol, max_iter=max_iter, mix_alpha=mixing,
+                                 precision=precision)
+        self.set_geometry(coords)
+
+    def set_geometry(self, coords, latvecs=None):
+        if latvecs is not None:
+            raise ValueError("periodic geometries are not supported by this engine")
+        self.coords = np.asarray(coords, dtype=np.float64)
+        self.ctx.set_geometry(self.coords, self.species)
+        self._res = None
+        self._grad = None
+
+    def _ensure(self):
+        if self._res is None:
+            self._res = self.ctx.scc(self.opts)
+
+    def get_nr_atoms(self) -> int:
+        return int(len(self.species))
+
+    def get_energy(self) -> float:
+        self._ensure()
+        return self._res["energies"]["EMermin"]
+
+    def get_energies(self) -> dict:
+        self._ensure()
+        return dict(self._res["energies"])
+
+    def get_gradients(self) -> np.ndarray:
+        """(natom, 3) gradients in Hartree/Bohr (same layout as DftbPlus.get_gradients)."""
+        self._ensure()
+        if self._grad is None:
+            self._grad = self.ctx.gradients().T.copy()
+        return self._grad
+
+    def get_gross_charges(self) -> np.ndarray:
+        self._ensure()
+        q0 = np.array([sum(self.model.species[s].occ) for s in self.species])
+        return q0 - self._res["q_out"]
+
+    def scc_info(self) -> dict:
+        self._ensure()
+        return dict(self._res)
+
+    def close(self):
+        self.ctx.close()

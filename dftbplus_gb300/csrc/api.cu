@@ -1,0 +1,653 @@
+// C-ABI of the dftbgpu library: context, model/geometry upload, the SCC driver and gradients.
+// Host orchestration only; all numerical work runs in the kernels of linalg.cu, stedc.cu and
+// dftb_kernels.cu on the context's stream.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "dftb_kernels.cuh"
+#include "linalg.cuh"
+
+namespace dg {
+
+long long g_launches = 0;
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  char err[1024] = {0};
+  // model
+  int nsp = 0;
+  std::vector<SpeciesDev> h_sp;
+  std::vector<PairDev> h_pair;
+  SpeciesDev *d_sp = nullptr;
+  PairDev *d_pair = nullptr;
+  double *d_tab = nullptr;
+  double *d_rep = nullptr;
+  double sk_cut_max = 0.0;
+  bool have_model = false;
+  // geometry
+  int natom = 0, norb = 0;
+  std::vector<int> h_species, h_orb_off;
+  double *d_xyz = nullptr;
+  int *d_species = nullptr;
+  int *d_orb = nullptr;       // orb_off[natom+1] then orb_atom[norb]
+  int *d_pcount = nullptr, *d_pstart = nullptr, *d_pi = nullptr, *d_pj = nullptr;
+  int npairs = 0;
+  size_t cap_atoms = 0, cap_pairs = 0;
+  bool have_geom = false;
+  // per-atom vectors
+  double *d_q0 = nullptr, *d_qin = nullptr, *d_qout = nullptr, *d_V = nullptr, *d_Vout = nullptr,
+         *d_eatom = nullptr, *d_grad = nullptr;
+  std::vector<double> h_q0;
+  // per-orbital vectors / matrices
+  size_t cap_n = 0;
+  double *H0 = nullptr, *S = nullptr, *Linv = nullptr, *H = nullptr, *T = nullptr, *Vh = nullptr,
+         *Z = nullptr, *C = nullptr, *rho = nullptr, *W = nullptr;
+  double *eig = nullptr, *fill = nullptr, *fe = nullptr, *dd = nullptr, *ee = nullptr, *tau = nullptr,
+         *qorb = nullptr, *eorb = nullptr;
+  double *wk_sytrd = nullptr, *wk_ormtr = nullptr, *wk_stedc = nullptr;
+  int *iwk_stedc = nullptr;
+  int *d_status = nullptr;
+  double *d_scal = nullptr;
+  // Broyden
+  int bro_cap_iter = 0;
+  size_t bro_cap_atoms = 0;
+  BroydenDev bro{};
+  // SCC state
+  bool have_scc = false;
+  int nlevels = 0;
+  bool have_w = false;
+  double nel = 0.0;
+};
+
+int set_error(Ctx *c, int code, const char *fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+template <class T>
+static int dev_alloc(Ctx *c, T **p, size_t count) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess)
+    return set_error(c, DFTBGPU_ERR_CUDA, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+  return DFTBGPU_OK;
+}
+
+// ------------------------------------------------------------------ host restatements (setup only)
+static double host_neville8(const double *col, double incr, double x, int il) {
+  double c[8], d[8], xp[8], delta[8];
+  for (int ii = 0; ii < 8; ++ii) {
+    xp[ii] = (double)(il - 8 + ii + 1) * incr;
+    c[ii] = d[ii] = col[il - 8 + ii];
+  }
+  for (int mm = 1; mm < 8; ++mm) delta[mm] = 1.0 / (xp[mm] - xp[0]);
+  int icl = (int)std::ceil((x - xp[0]) * delta[1]);
+  double y = col[il - 8 + icl - 1];
+  icl -= 1;
+  for (int mm = 1; mm < 8; ++mm) {
+    for (int i = 1; i <= 8 - mm; ++i) {
+      double r2 = (d[i - 1] - c[i]) * delta[mm];
+      c[i - 1] = (xp[i - 1] - x) * r2;
+      d[i - 1] = (xp[i - 1 + mm] - x) * r2;
+    }
+    double dy;
+    if (2 * icl < 8 - mm) dy = c[icl];
+    else { dy = d[icl - 1]; icl -= 1; }
+    y += dy;
+  }
+  return y;
+}
+
+static double host_gsub(double r, double t1, double t2) {
+  double t12 = t1 * t1 - t2 * t2;
+  return std::exp(-t1 * r) * ((0.5 * std::pow(t2, 4) * t1 / (t12 * t12)) -
+                              (std::pow(t2, 6) - 3.0 * std::pow(t2, 4) * t1 * t1) / (r * t12 * t12 * t12));
+}
+static double host_exp_gamma(double r, double ua, double ub) {
+  double ta = 3.2 * ua, tb = 3.2 * ub;
+  if (r < 1e-5) {
+    if (std::fabs(ua - ub) < 0.3125e-5) return -0.5 * (ua + ub);
+    return -0.5 * ((ta * tb) / (ta + tb) + (ta * tb) * (ta * tb) / std::pow(ta + tb, 3));
+  }
+  if (std::fabs(ua - ub) < 0.3125e-5) {
+    double tm = 0.5 * (ta + tb);
+    return std::exp(-tm * r) * (1.0 / r + 0.6875 * tm + 0.1875 * r * tm * tm +
+                                0.02083333333333333333 * r * r * tm * tm * tm);
+  }
+  return host_gsub(r, ta, tb) + host_gsub(r, tb, ta);
+}
+// shortgammafuncs.F90:27-94 (expGammaCutoff): distance where the short gamma drops below 1e-10.
+static double host_gamma_cutoff(double u2, double u1) {
+  const double cv = 1e-10, tol = 1e-10;
+  double rab = 1.0;
+  while (host_exp_gamma(rab, u2, u1) > cv) rab *= 2.0;
+  double min_cut = rab + 0.1, max_cut = 0.5 * rab - 0.1;
+  double max_g = host_exp_gamma(max_cut, u2, u1), min_g = host_exp_gamma(min_cut, u2, u1);
+  double lower_g = host_exp_gamma(min_cut, u2, u1);
+  double cut = max_cut + 0.1;
+  double g = host_exp_gamma(cut, u2, u1);
+  int guard = 0;
+  while ((g - lower_g) > tol && guard++ < 10000) {
+    max_cut = 0.5 * (cut + min_cut);
+    if ((max_g >= min_g) == (cv >= host_exp_gamma(max_cut, u2, u1))) {
+      min_cut = max_cut;
+      lower_g = host_exp_gamma(min_cut, u2, u1);
+    } else {
+      cut = max_cut;
+      g = host_exp_gamma(cut, u2, u1);
+    }
+  }
+  return min_cut;
+}
+
+// ------------------------------------------------------------------ buffers
+static int ensure_atoms(Ctx *c, int natom) {
+  if ((size_t)natom <= c->cap_atoms) return DFTBGPU_OK;
+  size_t n = natom;
+  DG_CHECK(c, dev_alloc(c, &c->d_xyz, 3 * n));
+  DG_CHECK(c, dev_alloc(c, &c->d_species, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_pcount, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_pstart, n + 1));
+  DG_CHECK(c, dev_alloc(c, &c->d_q0, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_qin, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_qout, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_V, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_Vout, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_eatom, n));
+  DG_CHECK(c, dev_alloc(c, &c->d_grad, 3 * n));
+  c->cap_atoms = n;
+  return DFTBGPU_OK;
+}
+
+static int ensure_orbitals(Ctx *c, int n) {
+  if ((size_t)n <= c->cap_n) return DFTBGPU_OK;
+  size_t nn = (size_t)n * n;
+  for (double **p : {&c->H0, &c->S, &c->Linv, &c->H, &c->T, &c->Vh, &c->Z, &c->C, &c->rho, &c->W})
+    DG_CHECK(c, dev_alloc(c, p, nn));
+  for (double **p : {&c->eig, &c->fill, &c->fe, &c->dd, &c->ee, &c->tau, &c->qorb, &c->eorb})
+    DG_CHECK(c, dev_alloc(c, p, (size_t)n));
+  DG_CHECK(c, dev_alloc(c, &c->wk_sytrd, sytrd_work_size(n)));
+  DG_CHECK(c, dev_alloc(c, &c->wk_ormtr, ormtr_work_size(n, n)));
+  DG_CHECK(c, dev_alloc(c, &c->wk_stedc, stedc_work_size(n)));
+  DG_CHECK(c, dev_alloc(c, &c->iwk_stedc, stedc_iwork_size(n)));
+  c->cap_n = n;
+  return DFTBGPU_OK;
+}
+
+static int ensure_broyden(Ctx *c, int natom, int max_iter) {
+  if (c->bro_cap_iter >= max_iter && c->bro_cap_atoms >= (size_t)natom) return DFTBGPU_OK;
+  int M = max_iter;
+  size_t N = natom;
+  DG_CHECK(c, dev_alloc(c, &c->bro.ww, M));
+  DG_CHECK(c, dev_alloc(c, &c->bro.aa, (size_t)M * M));
+  DG_CHECK(c, dev_alloc(c, &c->bro.dF, N * M));
+  DG_CHECK(c, dev_alloc(c, &c->bro.uu, N * M));
+  DG_CHECK(c, dev_alloc(c, &c->bro.qlast, N));
+  DG_CHECK(c, dev_alloc(c, &c->bro.dlast, N));
+  c->bro.max_iter = M;
+  c->bro_cap_iter = M;
+  c->bro_cap_atoms = N;
+  return DFTBGPU_OK;
+}
+
+static ModelDev model_view(Ctx *c) { return ModelDev{c->nsp, c->d_sp, c->d_pair, c->d_tab, c->d_rep}; }
+static GeomDev geom_view(Ctx *c) { return GeomDev{c->natom, c->norb, c->d_xyz, c->d_species, c->d_orb}; }
+
+static int check_status(Ctx *c, const char *stage) {
+  int st = 0;
+  DG_CUDA(c, cudaMemcpyAsync(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st == kDevNotPosDef) return set_error(c, DFTBGPU_ERR_NOT_POSDEF, "%s: overlap matrix is not positive definite", stage);
+  if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "%s: secular equation iteration cap reached", stage);
+  if (st != 0) return set_error(c, DFTBGPU_ERR_CUDA, "%s: device status %d", stage, st);
+  return DFTBGPU_OK;
+}
+
+// Generalized eigensolve of H (full symmetric, destroyed) with the stored L^-1. Eigenvalues into
+// c->eig; the eigenvectors of the first k levels into c->C (columns), k chosen by pick_k after the
+// eigenvalues are known (the Fermi filling decides how many levels the density matrix needs).
+template <class PickK>
+static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k) {
+  cudaStream_t s = c->stream;
+  // A = L^-1 H L^-T : T = H L^-T (L^-T upper), A(lower) = L^-1 T (L^-1 lower)
+  dgemm(s, 'N', 'T', n, n, n, 1.0, Hm, n, c->Linv, n, 0.0, c->T, n, kBUpper);
+  dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, Hm, n, kALower | kCLower);
+  sytrd_lower(s, n, Hm, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
+  int rc = stedc(s, n, c->dd, c->ee, c->Z, n, c->wk_stedc, c->iwk_stedc, c->d_status);
+  if (rc != 0) return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
+  DG_CUDA(c, cudaMemcpyAsync(c->eig, c->dd, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  int k = 0;
+  DG_CHECK(c, pick_k(&k));
+  if (k > 0) {
+    ormtr_left(s, n, k, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
+    dgemm(s, 'T', 'N', n, k, n, 1.0, c->Linv, n, c->Z, n, 0.0, c->C, n, kAUpper);
+  }
+  return DFTBGPU_OK;
+}
+
+static int density(Ctx *c, int n, int k, const double *w, double *out) {
+  cudaStream_t s = c->stream;
+  if (k <= 0) {
+    set_zero(s, out, (size_t)n * n);
+    return DFTBGPU_OK;
+  }
+  scale_columns(s, n, k, c->C, n, w, c->T, n);
+  dgemm(s, 'N', 'T', n, n, k, 1.0, c->T, n, c->C, n, 0.0, out, n, kCLower);
+  copy_lower_to_upper(s, n, out, n);
+  return DFTBGPU_OK;
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+struct dftbgpu_ctx : public dg::Ctx {};
+
+extern "C" {
+
+void dftbgpu_default_opts(dftbgpu_scc_opts *o) {
+  if (!o) return;
+  o->kT = 0.0;
+  o->scc_tol = 1e-5;
+  o->max_iter = 100;
+  o->min_iter = 1;
+  o->mix_alpha = 0.2;
+  o->mix_omega0 = 0.01;
+  o->mix_min_weight = 1.0;
+  o->mix_max_weight = 1e5;
+  o->mix_weight_fac = 1e-2;
+  o->net_charge = 0.0;
+  o->precision = DFTBGPU_PREC_FP64;
+  o->convergent_only = 0;
+}
+
+int dftbgpu_create(dftbgpu_ctx **out, int device) {
+  if (!out) return DFTBGPU_ERR_ARGS;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return DFTBGPU_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return DFTBGPU_ERR_ARGS;
+  dftbgpu_ctx *c = new dftbgpu_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return DFTBGPU_ERR_CUDA;
+  }
+  if (dev_alloc(c, &c->d_status, 4) || dev_alloc(c, &c->d_scal, kSCount)) {
+    delete c;
+    return DFTBGPU_ERR_CUDA;
+  }
+  cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+  *out = c;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_destroy(dftbgpu_ctx *c) {
+  if (!c) return DFTBGPU_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  void *ptrs[] = {c->d_sp, c->d_pair, c->d_tab, c->d_rep, c->d_xyz, c->d_species, c->d_orb, c->d_pcount,
+                  c->d_pstart, c->d_pi, c->d_pj, c->d_q0, c->d_qin, c->d_qout, c->d_V, c->d_Vout,
+                  c->d_eatom, c->d_grad, c->H0, c->S, c->Linv, c->H, c->T, c->Vh, c->Z, c->C, c->rho,
+                  c->W, c->eig, c->fill, c->fe, c->dd, c->ee, c->tau, c->qorb, c->eorb, c->wk_sytrd,
+                  c->wk_ormtr, c->wk_stedc, c->iwk_stedc, c->d_status, c->d_scal, c->bro.ww, c->bro.aa,
+                  c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return DFTBGPU_OK;
+}
+
+const char *dftbgpu_last_error(const dftbgpu_ctx *c) { return c ? c->err : "null context"; }
+
+long long dftbgpu_kernel_launches(const dftbgpu_ctx *) { return dg::g_launches; }
+
+int dftbgpu_set_model(dftbgpu_ctx *c, int nsp, const int *n_shell, const int *ang_shell, const double *onsite,
+                      const double *hubbu, const double *ref_occ, const double *sk_dist, const int *sk_rows,
+                      const int *sk_nint, const double *sk_ham, const double *sk_over, const int *rep_nspline,
+                      const double *rep_data) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (nsp <= 0 || !n_shell || !ang_shell || !onsite || !hubbu || !ref_occ || !sk_dist || !sk_rows || !sk_nint ||
+      !sk_ham || !sk_over || !rep_nspline || !rep_data)
+    return set_error(c, DFTBGPU_ERR_ARGS, "set_model: null argument or nsp <= 0");
+  cudaSetDevice(c->device);
+  c->nsp = nsp;
+  c->h_sp.assign(nsp, SpeciesDev{});
+  for (int a = 0; a < nsp; ++a) {
+    SpeciesDev &sp = c->h_sp[a];
+    sp.n_shell = n_shell[a];
+    if (sp.n_shell < 1 || sp.n_shell > kMaxShell)
+      return set_error(c, DFTBGPU_ERR_ARGS, "species %d: %d shells (1..%d supported)", a, sp.n_shell, kMaxShell);
+    sp.n_orb = 0;
+    for (int k = 0; k < kMaxShell; ++k) {
+      sp.ang[k] = (k < sp.n_shell) ? ang_shell[a * kMaxShell + k] : -1;
+      sp.onsite[k] = onsite[a * kMaxShell + k];
+      sp.occ[k] = ref_occ[a * kMaxShell + k];
+      if (k < sp.n_shell) {
+        if (sp.ang[k] < 0 || sp.ang[k] > 2)
+          return set_error(c, DFTBGPU_ERR_ARGS, "species %d shell %d: l=%d (s, p, d supported)", a, k, sp.ang[k]);
+        sp.n_orb += 2 * sp.ang[k] + 1;
+      }
+    }
+    if (sp.n_orb > kMaxOrb) return set_error(c, DFTBGPU_ERR_ARGS, "species %d: %d orbitals > %d", a, sp.n_orb, kMaxOrb);
+    sp.hubbu = hubbu[a];
+    if (!(sp.hubbu > 1e-6)) return set_error(c, DFTBGPU_ERR_ARGS, "species %d: Hubbard U too small", a);
+  }
+  c->h_pair.assign((size_t)nsp * nsp, PairDev{});
+  long long off = 0, roff = 0;
+  long long ham_off = 0;
+  for (int p = 0; p < nsp * nsp; ++p) ham_off += (long long)sk_rows[p] * sk_nint[p];
+  std::vector<double> tab(2 * (size_t)ham_off);
+  std::memcpy(tab.data(), sk_ham, sizeof(double) * ham_off);
+  std::memcpy(tab.data() + ham_off, sk_over, sizeof(double) * ham_off);
+  long long rep_total = 0;
+  for (int p = 0; p < nsp * nsp; ++p) rep_total += 4 + rep_nspline[p] + 4LL * (rep_nspline[p] - 1) + 6;
+  c->sk_cut_max = 0.0;
+  for (int a = 0; a < nsp; ++a)
+    for (int b = 0; b < nsp; ++b) {
+      int p = a * nsp + b;
+      PairDev &P = c->h_pair[p];
+      P.dist = sk_dist[p];
+      P.rows = sk_rows[p];
+      P.n_int = sk_nint[p];
+      int want = 0;
+      for (int i = 0; i < c->h_sp[a].n_shell; ++i)
+        for (int j = 0; j < c->h_sp[b].n_shell; ++j) want += std::min(c->h_sp[a].ang[i], c->h_sp[b].ang[j]) + 1;
+      if (P.n_int != want || P.n_int > kMaxInt)
+        return set_error(c, DFTBGPU_ERR_ARGS, "pair %d-%d: %d integrals, expected %d", a, b, P.n_int, want);
+      if (P.rows < 9 || !(P.dist > 0))
+        return set_error(c, DFTBGPU_ERR_ARGS, "pair %d-%d: not enough points in the SK table", a, b);
+      P.off_ham = off;
+      P.off_over = ham_off + off;
+      P.sk_cut = P.rows * P.dist + 1.0;
+      c->sk_cut_max = std::max(c->sk_cut_max, P.sk_cut);
+      // 5th-order tail coefficients (slakoeqgrid.F90:225-241), per integral
+      for (int k = 0; k < P.n_int; ++k) {
+        for (int m = 0; m < 2; ++m) {
+          const double *col = tab.data() + (m ? P.off_over : P.off_ham) + (size_t)k * P.rows;
+          double xa8 = (double)P.rows * P.dist;
+          double y0 = host_neville8(col, P.dist, xa8 - 1e-5, P.rows);
+          double y2 = host_neville8(col, P.dist, xa8 + 1e-5, P.rows);
+          double y1 = col[P.rows - 1];
+          double (*tl)[kMaxInt] = m ? P.tail_s : P.tail_h;
+          tl[0][k] = y1;
+          tl[1][k] = (y2 - y0) / (2.0 * 1e-5);
+          tl[2][k] = (y2 + y0 - 2.0 * y1) / (1e-5 * 1e-5);
+        }
+      }
+      off += (long long)P.rows * P.n_int;
+      P.off_rep = roff;
+      P.n_spline = rep_nspline[p];
+      P.rep_cut = rep_data[roff];
+      roff += 4 + P.n_spline + 4LL * (P.n_spline - 1) + 6;
+      P.gamma_cut = host_gamma_cutoff(c->h_sp[b].hubbu, c->h_sp[a].hubbu);
+    }
+  DG_CHECK(c, dev_alloc(c, &c->d_sp, (size_t)nsp));
+  DG_CHECK(c, dev_alloc(c, &c->d_pair, (size_t)nsp * nsp));
+  DG_CHECK(c, dev_alloc(c, &c->d_tab, tab.size()));
+  DG_CHECK(c, dev_alloc(c, &c->d_rep, (size_t)rep_total));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_sp, c->h_sp.data(), sizeof(SpeciesDev) * nsp, cudaMemcpyHostToDevice, c->stream));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_pair, c->h_pair.data(), sizeof(PairDev) * nsp * nsp, cudaMemcpyHostToDevice, c->stream));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, c->stream));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_rep, rep_data, sizeof(double) * rep_total, cudaMemcpyHostToDevice, c->stream));
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_model = true;
+  c->have_geom = false;
+  c->have_scc = false;
+  return DFTBGPU_OK;
+}
+
+static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bool dev, const int *species) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (!c->have_model) return set_error(c, DFTBGPU_ERR_STATE, "set_geometry: no model set");
+  if (natom <= 0 || !coords || !species) return set_error(c, DFTBGPU_ERR_ARGS, "set_geometry: bad arguments");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  c->h_species.assign(species, species + natom);
+  c->h_orb_off.assign(natom + 1, 0);
+  c->h_q0.assign(natom, 0.0);
+  for (int a = 0; a < natom; ++a) {
+    int sp = species[a];
+    if (sp < 0 || sp >= c->nsp) return set_error(c, DFTBGPU_ERR_ARGS, "atom %d: species %d out of range", a, sp);
+    c->h_orb_off[a + 1] = c->h_orb_off[a] + c->h_sp[sp].n_orb;
+    double q = 0.0;
+    for (int k = 0; k < c->h_sp[sp].n_shell; ++k) q += c->h_sp[sp].occ[k];
+    c->h_q0[a] = q;
+  }
+  int norb = c->h_orb_off[natom];
+  DG_CHECK(c, ensure_atoms(c, natom));
+  DG_CHECK(c, ensure_orbitals(c, norb));
+  DG_CHECK(c, dev_alloc(c, &c->d_orb, (size_t)natom + 1 + norb));
+  std::vector<int> orb(natom + 1 + norb);
+  for (int a = 0; a <= natom; ++a) orb[a] = c->h_orb_off[a];
+  for (int a = 0; a < natom; ++a)
+    for (int o = c->h_orb_off[a]; o < c->h_orb_off[a + 1]; ++o) orb[natom + 1 + o] = a;
+  c->natom = natom;
+  c->norb = norb;
+  DG_CUDA(c, cudaMemcpyAsync(c->d_orb, orb.data(), sizeof(int) * orb.size(), cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_species, species, sizeof(int) * natom, cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_xyz, coords, sizeof(double) * 3 * natom,
+                             dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemcpyAsync(c->d_q0, c->h_q0.data(), sizeof(double) * natom, cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  GeomDev g = geom_view(c);
+  ModelDev m = model_view(c);
+  // neighbour list (pairs within the SK cutoff); the pair arrays grow on demand
+  int np = 0;
+  {
+    // count first to size the arrays
+    size_t need = (size_t)natom * 64;
+    if (c->cap_pairs < need) {
+      DG_CHECK(c, dev_alloc(c, &c->d_pi, need));
+      DG_CHECK(c, dev_alloc(c, &c->d_pj, need));
+      c->cap_pairs = need;
+    }
+    build_pairs(s, g, c->sk_cut_max, c->d_pcount, c->d_pstart, c->d_pi, c->d_pj, c->cap_pairs, &np);
+    if ((size_t)np > c->cap_pairs) {
+      DG_CHECK(c, dev_alloc(c, &c->d_pi, (size_t)np));
+      DG_CHECK(c, dev_alloc(c, &c->d_pj, (size_t)np));
+      c->cap_pairs = np;
+      build_pairs(s, g, c->sk_cut_max, c->d_pcount, c->d_pstart, c->d_pi, c->d_pj, c->cap_pairs, &np);
+    }
+  }
+  c->npairs = np;
+  build_h0_s(s, m, g, c->d_pi, c->d_pj, np, c->H0, c->S);
+  repulsive_energy(s, m, g, c->d_eatom, c->d_scal);
+  // Cholesky of S (in Z as scratch) and L^-1
+  DG_CUDA(c, cudaMemcpyAsync(c->Z, c->S, sizeof(double) * (size_t)norb * norb, cudaMemcpyDeviceToDevice, s));
+  potrf_lower(s, norb, c->Z, norb, c->d_status);
+  DG_CHECK(c, check_status(c, "Cholesky of S"));
+  trtri_lower(s, norb, c->Z, norb, c->Linv, norb, c->T);
+  DG_CUDA(c, cudaGetLastError());
+  DG_CUDA(c, cudaStreamSynchronize(s));
+  c->have_geom = true;
+  c->have_scc = false;
+  c->have_w = false;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_set_geometry(dftbgpu_ctx *c, int natom, const double *coords, const int *species) {
+  return set_geometry_impl(c, natom, coords, false, species);
+}
+
+int dftbgpu_set_geometry_dev(dftbgpu_ctx *c, int natom, const double *coords_dev, const int *species_host) {
+  return set_geometry_impl(c, natom, coords_dev, true, species_host);
+}
+
+int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init, dftbgpu_energies *energies,
+                double *ef, double *eigen, double *filling, double *q_out, int *n_iter, int *converged) {
+  if (!c || !o) return DFTBGPU_ERR_ARGS;
+  if (!c->have_geom) return set_error(c, DFTBGPU_ERR_STATE, "scc: no geometry set");
+  if (o->max_iter < 1 || o->max_iter > 150) return set_error(c, DFTBGPU_ERR_ARGS, "scc: max_iter must be in 1..150");
+  if (!(o->kT > 0.0)) return set_error(c, DFTBGPU_ERR_ARGS, "scc: kT must be > 0 (Fermi filling)");
+  if (o->precision != DFTBGPU_PREC_FP64) return set_error(c, DFTBGPU_ERR_ARGS, "scc: precision form %d not available", o->precision);
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n = c->norb, N = c->natom;
+  GeomDev g = geom_view(c);
+  ModelDev m = model_view(c);
+  DG_CHECK(c, ensure_broyden(c, N, o->max_iter));
+  double nel = 0.0;
+  for (double q : c->h_q0) nel += q;
+  nel -= o->net_charge;
+  c->nel = nel;
+  if (q_init) DG_CUDA(c, cudaMemcpyAsync(c->d_qin, q_init, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+  else DG_CUDA(c, cudaMemcpyAsync(c->d_qin, c->d_q0, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+  DG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  double h_scal[kSCount];
+  int it = 0;
+  bool conv = false;
+  for (it = 1; it <= o->max_iter; ++it) {
+    potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
+    assemble_h(s, g, c->H0, c->S, c->d_V, c->H);
+    int k = 0;
+    auto pick = [&](int *kout) -> int {
+      fermi_filling(s, n, c->eig, nel, o->kT, c->fill, c->d_scal);
+      DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
+      DG_CUDA(c, cudaStreamSynchronize(s));
+      int st = 0;
+      DG_CUDA(c, cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+      if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "eigensolver: secular iteration cap reached");
+      if (h_scal[kSFermiStatus] != 0.0) return set_error(c, DFTBGPU_ERR_FERMI, "Fermi level search did not converge.");
+      *kout = (int)h_scal[kSNLevels];
+      return DFTBGPU_OK;
+    };
+    DG_CHECK(c, eigensolve(c, n, c->H, pick));
+    k = (int)h_scal[kSNLevels];
+    c->nlevels = k;
+    DG_CHECK(c, density(c, n, k, c->fill, c->rho));
+    mulliken(s, g, c->rho, c->S, c->H0, c->qorb, c->d_qout, c->eorb, c->d_scal);
+    potential(s, m, g, c->d_qout, c->d_q0, c->d_Vout);
+    scc_energy(s, N, c->d_Vout, c->d_qout, c->d_q0, c->d_scal);
+    broyden_step(s, N, it, o->min_iter, o->max_iter, o->scc_tol, o->mix_alpha, o->mix_omega0, o->mix_min_weight,
+                 o->mix_max_weight, o->mix_weight_fac, c->bro, c->d_qin, c->d_qout, c->d_scal);
+    DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(c, cudaStreamSynchronize(s));
+    DG_CUDA(c, cudaGetLastError());
+    conv = h_scal[kSConv] != 0.0;
+    if (conv) break;
+  }
+  if (it > o->max_iter) it = o->max_iter;
+  c->have_scc = true;
+  c->have_w = false;
+  if (energies) {
+    energies->EnonSCC = h_scal[kSEnonScc];
+    energies->Escc = h_scal[kSEscc];
+    energies->Erep = h_scal[kSErep];
+    energies->Eband = h_scal[kSEband];
+    energies->TS = h_scal[kSTS];
+    energies->E0 = h_scal[kSE0];
+    energies->Etotal = h_scal[kSEnonScc] + h_scal[kSEscc] + h_scal[kSErep];
+    energies->EMermin = energies->Etotal - h_scal[kSTS];
+  }
+  if (ef) *ef = h_scal[kSEf];
+  if (eigen) DG_CUDA(c, cudaMemcpy(eigen, c->eig, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (filling) DG_CUDA(c, cudaMemcpy(filling, c->fill, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (q_out) DG_CUDA(c, cudaMemcpy(q_out, c->d_qout, sizeof(double) * N, cudaMemcpyDeviceToHost));
+  if (n_iter) *n_iter = it;
+  if (converged) *converged = conv ? 1 : 0;
+  if (!conv && o->convergent_only)
+    return set_error(c, DFTBGPU_ERR_SCC_NOT_CONVERGED, "SCC is NOT converged, maximal SCC iterations exceeded");
+  return DFTBGPU_OK;
+}
+
+static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
+  if (!c || !grad) return DFTBGPU_ERR_ARGS;
+  if (!c->have_scc) return set_error(c, DFTBGPU_ERR_STATE, "gradients: call dftbgpu_scc first");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n = c->norb;
+  energy_weights(s, c->nlevels, c->fill, c->eig, c->fe);
+  DG_CHECK(c, density(c, n, c->nlevels, c->fe, c->W));
+  c->have_w = true;
+  GeomDev g = geom_view(c);
+  ModelDev m = model_view(c);
+  gradient_bands(s, m, g, c->rho, c->W, c->d_Vout, c->d_grad);
+  gradient_dc_rep(s, m, g, c->d_qout, c->d_q0, c->d_grad);
+  DG_CUDA(c, cudaGetLastError());
+  if (dev) {
+    DG_CUDA(c, cudaMemcpyAsync(grad, c->d_grad, sizeof(double) * 3 * c->natom, cudaMemcpyDeviceToDevice, s));
+    DG_CUDA(c, cudaStreamSynchronize(s));
+  } else {
+    DG_CUDA(c, cudaMemcpyAsync(grad, c->d_grad, sizeof(double) * 3 * c->natom, cudaMemcpyDeviceToHost, s));
+    DG_CUDA(c, cudaStreamSynchronize(s));
+  }
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_gradients(dftbgpu_ctx *c, double *grad) { return gradients_impl(c, grad, false); }
+int dftbgpu_gradients_dev(dftbgpu_ctx *c, double *grad_dev) { return gradients_impl(c, grad_dev, true); }
+
+int dftbgpu_n_orbitals(const dftbgpu_ctx *c, int *n_orb) {
+  if (!c || !n_orb) return DFTBGPU_ERR_ARGS;
+  *n_orb = c->norb;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_get_orbital_populations(dftbgpu_ctx *c, double *q_orb) {
+  if (!c || !q_orb) return DFTBGPU_ERR_ARGS;
+  if (!c->have_scc) return set_error(c, DFTBGPU_ERR_STATE, "no SCC result");
+  DG_CUDA(c, cudaMemcpy(q_orb, c->qorb, sizeof(double) * c->norb, cudaMemcpyDeviceToHost));
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_get_matrix(dftbgpu_ctx *c, int which, double *out) {
+  if (!c || !out) return DFTBGPU_ERR_ARGS;
+  if (!c->have_geom) return set_error(c, DFTBGPU_ERR_STATE, "no geometry");
+  const double *src = nullptr;
+  switch (which) {
+    case 0: src = c->H0; break;
+    case 1: src = c->S; break;
+    case 2: src = c->have_scc ? c->rho : nullptr; break;
+    case 3: src = nullptr; break;
+    case 4: src = c->have_w ? c->W : nullptr; break;
+    default: break;
+  }
+  if (!src) return set_error(c, DFTBGPU_ERR_STATE, "matrix %d not available", which);
+  cudaSetDevice(c->device);
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  DG_CUDA(c, cudaMemcpy(out, src, sizeof(double) * (size_t)c->norb * c->norb, cudaMemcpyDeviceToHost));
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_sygvd(dftbgpu_ctx *c, int n, double *a, double *b, double *w) {
+  if (!c || !a || !b || !w || n <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  DG_CHECK(c, ensure_orbitals(c, n));
+  size_t nn = (size_t)n * n;
+  DG_CUDA(c, cudaMemcpyAsync(c->H, a, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemcpyAsync(c->Z, b, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  DG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  potrf_lower(s, n, c->Z, n, c->d_status);
+  DG_CHECK(c, check_status(c, "sygvd Cholesky"));
+  // the caller's b receives L; keep a copy because Z is reused by the tridiagonal solver
+  DG_CUDA(c, cudaMemcpyAsync(b, c->Z, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
+  trtri_lower(s, n, c->Z, n, c->Linv, n, c->T);
+  // the SCC state (if any) no longer matches the stored L^-1
+  c->have_geom = false;
+  c->have_scc = false;
+  auto pick = [&](int *k) -> int {
+    *k = n;
+    return DFTBGPU_OK;
+  };
+  DG_CHECK(c, eigensolve(c, n, c->H, pick));
+  DG_CHECK(c, check_status(c, "sygvd eigensolver"));
+  DG_CUDA(c, cudaMemcpyAsync(w, c->eig, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  DG_CUDA(c, cudaMemcpyAsync(a, c->C, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
+  DG_CUDA(c, cudaStreamSynchronize(s));
+  return DFTBGPU_OK;
+}
+
+}  // extern "C"

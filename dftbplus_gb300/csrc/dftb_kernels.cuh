@@ -1,0 +1,67 @@
+// DFTB-specific kernels (SK tables, electrostatics, filling, mixing, forces).
+#pragma once
+#include "common.cuh"
+
+namespace dg {
+
+struct ModelDev {
+  int nsp;
+  const SpeciesDev *sp;     // [nsp]
+  const PairDev *pair;      // [nsp*nsp]
+  const double *tab;        // SK tables (H and S), offsets in PairDev
+  const double *rep;        // repulsive data
+};
+
+struct GeomDev {
+  int natom;
+  int norb;
+  const double *xyz;        // [3*natom]
+  const int *species;       // [natom]
+  const int *orb_off;       // [natom+1]
+};
+
+// Device scalars written by the SCC kernels (index into a small double array).
+enum Scalar : int {
+  kSEf = 0, kSEband, kSTS, kSE0, kSEnonScc, kSEscc, kSErep, kSErr, kSNel, kSConv,
+  kSNLevels, kSFermiStatus, kSCount = 16
+};
+
+// pair list
+// Half neighbour list (i < j, r <= cutoff) in CSR order; fills pi/pj only if npairs <= cap.
+void build_pairs(cudaStream_t s, const GeomDev &g, double cutoff, int *count, int *start, int *pi, int *pj,
+                 size_t cap, int *npairs_host);
+// H0 / S (dense, full symmetric)
+void build_h0_s(cudaStream_t s, const ModelDev &m, const GeomDev &g, const int *start, const int *pj,
+                int npairs, double *H0, double *S);
+// repulsive energy (per atom, then summed into scal[kSErep])
+void repulsive_energy(cudaStream_t s, const ModelDev &m, const GeomDev &g, double *eatom, double *scal);
+// atom potential V = 1/r dq - gamma_short dq from atom populations q and reference q0
+void potential(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double *q, const double *q0,
+               double *V);
+// H = H0 + 1/2 S (V_mu + V_nu)
+void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double *S, const double *V,
+                double *H);
+// Fermi filling (spin unpolarised) from ascending eigenvalues; writes fill[n], scal[...]
+void fermi_filling(cudaStream_t s, int n, const double *eig, double nel, double kT, double *fill,
+                   double *scal);
+// Mulliken populations per orbital and atom + Tr(rho H0) into scal[kSEnonScc]
+void mulliken(cudaStream_t s, const GeomDev &g, const double *rho, const double *S, const double *H0,
+              double *qorb, double *qatom, double *eorb, double *scal);
+// E_SCC = 1/2 sum V_A dq_A
+void scc_energy(cudaStream_t s, int natom, const double *V, const double *q, const double *q0, double *scal);
+// Broyden mixing on device (single CTA); returns nothing, writes scal[kSErr], scal[kSConv], qin.
+struct BroydenDev {
+  int max_iter;
+  double *ww, *aa, *dF, *uu, *qlast, *dlast;
+};
+void broyden_step(cudaStream_t s, int natom, int it, int min_iter, int max_iter_scc, double tol,
+                  double alpha, double omega0, double minw, double maxw, double wfac,
+                  BroydenDev b, double *qin, const double *qout, double *scal);
+// gradients
+void gradient_bands(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double *rho,
+                    const double *W, const double *V, double *grad);
+void gradient_dc_rep(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double *q,
+                     const double *q0, double *grad);
+void energy_weights(cudaStream_t s, int k, const double *fill, const double *eig, double *fe);
+
+}  // namespace dg

@@ -1,0 +1,640 @@
+// FP64 dense kernels: GEMM with triangular skipping, blocked Cholesky, triangular inverse,
+// blocked Householder tridiagonalisation (lower) and its back-transformation.
+//
+// These replace the LAPACK/MAGMA calls behind hegvd/magmaHegvd (math/eigensolver.F90:561-660,
+// :1143-1245): potrf + sygst are expressed as a Cholesky factor L, its inverse X = L^-1 and two
+// GEMMs (A = X H X^T), sytrd/ormtr as below, the tridiagonal solve lives in stedc.cu.
+#include "linalg.cuh"
+
+namespace dg {
+
+// ------------------------------------------------------------------------------------- GEMM
+// 64x64 output tile per CTA, 256 threads, 4x4 outputs per thread (strided by 16 so that shared
+// memory reads are conflict-free), K step 16, register prefetch of the next K slab.
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double alpha,
+                                                    const double *__restrict__ A, int lda,
+                                                    const double *__restrict__ B, int ldb,
+                                                    double beta, double *__restrict__ C, int ldc,
+                                                    int flags) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int i0 = blockIdx.x * BM, j0 = blockIdx.y * BN;
+  if ((flags & kCLower) && i0 + BM - 1 < j0) return;
+  int kmin = 0, kmax = k;
+  if (flags & kALower) kmax = min(kmax, i0 + BM);
+  if (flags & kAUpper) kmin = max(kmin, i0);
+  if (flags & kBLower) kmin = max(kmin, j0);
+  if (flags & kBUpper) kmax = min(kmax, j0 + BN);
+
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  double ra[4], rb[4];
+  auto load_a = [&](int p0) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int t = tid + 256 * r;
+      int ii, pp;
+      if (!TA) { ii = t & 63; pp = t >> 6; } else { pp = t & 15; ii = t >> 4; }
+      int gi = i0 + ii, gp = p0 + pp;
+      double v = 0.0;
+      if (gi < m && gp < kmax) v = TA ? A[gp + (size_t)gi * lda] : A[gi + (size_t)gp * lda];
+      ra[r] = v;
+    }
+  };
+  auto load_b = [&](int p0) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int t = tid + 256 * r;
+      int pp, jj;
+      if (!TB) { pp = t & 15; jj = t >> 4; } else { jj = t & 63; pp = t >> 6; }
+      int gj = j0 + jj, gp = p0 + pp;
+      double v = 0.0;
+      if (gj < n && gp < kmax) v = TB ? B[gj + (size_t)gp * ldb] : B[gp + (size_t)gj * ldb];
+      rb[r] = v;
+    }
+  };
+  auto store_ab = [&]() {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int t = tid + 256 * r;
+      int ii, pp;
+      if (!TA) { ii = t & 63; pp = t >> 6; } else { pp = t & 15; ii = t >> 4; }
+      As[pp][ii] = ra[r];
+      int jj, qq;
+      if (!TB) { qq = t & 15; jj = t >> 4; } else { jj = t & 63; qq = t >> 6; }
+      Bs[qq][jj] = rb[r];
+    }
+  };
+
+  if (kmin < kmax) {
+    load_a(kmin);
+    load_b(kmin);
+    for (int p0 = kmin; p0 < kmax; p0 += BK) {
+      __syncthreads();
+      store_ab();
+      __syncthreads();
+      if (p0 + BK < kmax) {
+        load_a(p0 + BK);
+        load_b(p0 + BK);
+      }
+#pragma unroll
+      for (int pp = 0; pp < BK; ++pp) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[pp][tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[pp][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int gi = i0 + tx + 16 * i;
+    if (gi >= m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gj = j0 + ty + 16 * j;
+      if (gj >= n) continue;
+      double *c = C + gi + (size_t)gj * ldc;
+      double v = alpha * acc[i][j];
+      if (beta != 0.0) v = fma(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+
+void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
+           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags) {
+  if (m <= 0 || n <= 0) return;
+  dim3 grid(ceil_div(m, 64), ceil_div(n, 64));
+  bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  if (!TA && !TB)
+    dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+  else if (!TA && TB)
+    dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+  else if (TA && !TB)
+    dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+  else
+    dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+  count_launch();
+}
+
+// ------------------------------------------------------------------------------------- helpers
+__global__ void set_zero_kernel(double *p, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = 0.0;
+}
+void set_zero(cudaStream_t s, double *p, size_t n) {
+  if (!n) return;
+  int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  set_zero_kernel<<<blocks, 256, 0, s>>>(p, n);
+  count_launch();
+}
+
+// 32x32 tiles through shared memory so both the read (lower) and the write (upper) are coalesced.
+__global__ void lower_to_upper_kernel(int n, double *A, int lda) {
+  __shared__ double t[32][33];
+  int bi = blockIdx.x, bj = blockIdx.y;  // tile (bi, bj) with bi >= bj in the lower triangle
+  if (bi < bj) return;
+  int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    int gi = bi * 32 + tx, gj = bj * 32 + r;
+    t[r][tx] = (gi < n && gj < n) ? A[gi + (size_t)gj * lda] : 0.0;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    int gi = bj * 32 + tx, gj = bi * 32 + r;   // write A(gi, gj) = A(gj, gi) for gj > gi
+    if (gi < n && gj < n && gj > gi) A[gi + (size_t)gj * lda] = t[tx][r];
+  }
+}
+void copy_lower_to_upper(cudaStream_t s, int n, double *A, int lda) {
+  dim3 g(ceil_div(n, 32), ceil_div(n, 32));
+  lower_to_upper_kernel<<<g, dim3(32, 8), 0, s>>>(n, A, lda);
+  count_launch();
+}
+
+__global__ void zero_upper_kernel(int n, double *A, int lda) {
+  int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < j && i < n; i += gridDim.x * blockDim.x)
+    A[i + (size_t)j * lda] = 0.0;
+}
+void zero_strict_upper(cudaStream_t s, int n, double *A, int lda) {
+  dim3 g(ceil_div(n, 256), n);
+  zero_upper_kernel<<<g, 256, 0, s>>>(n, A, lda);
+  count_launch();
+}
+
+__global__ void scale_columns_kernel(int m, int n, const double *A, int lda, const double *f, double *B,
+                                     int ldb) {
+  int j = blockIdx.y;
+  double fj = f[j];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    B[i + (size_t)j * ldb] = A[i + (size_t)j * lda] * fj;
+}
+void scale_columns(cudaStream_t s, int m, int n, const double *A, int lda, const double *f, double *B,
+                   int ldb) {
+  if (m <= 0 || n <= 0) return;
+  dim3 g(std::min(ceil_div(m, 256), 8), n);
+  scale_columns_kernel<<<g, 256, 0, s>>>(m, n, A, lda, f, B, ldb);
+  count_launch();
+}
+
+// ------------------------------------------------------------------------------------- Cholesky
+constexpr int NB = 64;
+
+// Unblocked Cholesky of one jb x jb diagonal block in shared memory.
+__global__ void potf2_kernel(int jb, double *A, int lda, int *status) {
+  __shared__ double a[NB][NB + 1];
+  const int t = threadIdx.x;
+  for (int idx = t; idx < jb * jb; idx += blockDim.x) {
+    int r = idx % jb, c = idx / jb;
+    a[r][c] = (r >= c) ? A[r + (size_t)c * lda] : 0.0;
+  }
+  __syncthreads();
+  for (int c = 0; c < jb; ++c) {
+    double piv = a[c][c];
+    bool bad = !(piv > 0.0) || !isfinite(piv);
+    if (bad && t == 0) atomicExch(status, kDevNotPosDef);
+    double sq = sqrt(bad ? 1.0 : piv);
+    __syncthreads();
+    if (t == 0) a[c][c] = sq;
+    for (int r = c + 1 + t; r < jb; r += blockDim.x) a[r][c] /= sq;
+    __syncthreads();
+    int mr = jb - c - 1;
+    for (int idx = t; idx < mr * mr; idx += blockDim.x) {
+      int r = c + 1 + idx % mr, q = c + 1 + idx / mr;
+      if (r >= q) a[r][q] = fma(-a[r][c], a[q][c], a[r][q]);
+    }
+    __syncthreads();
+  }
+  for (int idx = t; idx < jb * jb; idx += blockDim.x) {
+    int r = idx % jb, c = idx / jb;
+    A[r + (size_t)c * lda] = (r >= c) ? a[r][c] : 0.0;
+  }
+}
+
+// Solve X L11^T = B for the panel rows below the diagonal block (B overwritten by X).
+__global__ void trsm_panel_kernel(int m, int jb, const double *L, int ldl, double *B, int ldb) {
+  __shared__ double l[NB][NB + 1];
+  __shared__ double x[NB][NB + 1];
+  const int t = threadIdx.x;
+  const int r0 = blockIdx.x * NB;
+  for (int idx = t; idx < jb * jb; idx += blockDim.x) {
+    int r = idx % jb, c = idx / jb;
+    l[r][c] = (r >= c) ? L[r + (size_t)c * ldl] : 0.0;
+  }
+  for (int idx = t; idx < NB * jb; idx += blockDim.x) {
+    int r = idx % NB, c = idx / NB;
+    x[r][c] = (r0 + r < m) ? B[r0 + r + (size_t)c * ldb] : 0.0;
+  }
+  __syncthreads();
+  if (t < NB && r0 + t < m) {
+    for (int c = 0; c < jb; ++c) {
+      double v = x[t][c];
+      for (int q = 0; q < c; ++q) v = fma(-x[t][q], l[c][q], v);
+      x[t][c] = v / l[c][c];
+    }
+  }
+  __syncthreads();
+  for (int idx = t; idx < NB * jb; idx += blockDim.x) {
+    int r = idx % NB, c = idx / NB;
+    if (r0 + r < m) B[r0 + r + (size_t)c * ldb] = x[r][c];
+  }
+}
+
+void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev) {
+  for (int j0 = 0; j0 < n; j0 += NB) {
+    int jb = std::min(NB, n - j0);
+    double *Ajj = A + j0 + (size_t)j0 * lda;
+    potf2_kernel<<<1, 256, 0, s>>>(jb, Ajj, lda, status_dev);
+    count_launch();
+    int m = n - j0 - jb;
+    if (m > 0) {
+      double *B = A + j0 + jb + (size_t)j0 * lda;
+      trsm_panel_kernel<<<ceil_div(m, NB), 256, 0, s>>>(m, jb, Ajj, lda, B, lda);
+      count_launch();
+      double *A22 = A + j0 + jb + (size_t)(j0 + jb) * lda;
+      dgemm(s, 'N', 'T', m, m, jb, -1.0, B, lda, B, lda, 1.0, A22, lda, kCLower);
+    }
+  }
+  zero_strict_upper(s, n, A, lda);
+}
+
+// ------------------------------------------------------------------------------------- L^-1
+__global__ void trtri_diag_kernel(int n, const double *L, int ldl, double *X, int ldx) {
+  __shared__ double l[NB][NB + 1];
+  __shared__ double x[NB][NB + 1];
+  const int j0 = blockIdx.x * NB;
+  const int jb = min(NB, n - j0);
+  const int t = threadIdx.x;
+  for (int idx = t; idx < jb * jb; idx += blockDim.x) {
+    int r = idx % jb, c = idx / jb;
+    l[r][c] = (r >= c) ? L[j0 + r + (size_t)(j0 + c) * ldl] : 0.0;
+    x[r][c] = 0.0;
+  }
+  __syncthreads();
+  if (t < jb) {
+    for (int r = t; r < jb; ++r) {
+      double v = (r == t) ? 1.0 : 0.0;
+      for (int q = t; q < r; ++q) v = fma(-l[r][q], x[q][t], v);
+      x[r][t] = v / l[r][r];
+    }
+  }
+  __syncthreads();
+  for (int idx = t; idx < jb * jb; idx += blockDim.x) {
+    int r = idx % jb, c = idx / jb;
+    X[j0 + r + (size_t)(j0 + c) * ldx] = x[r][c];
+  }
+}
+
+void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work) {
+  // X must start zero outside the blocks that are written.
+  set_zero(s, X, (size_t)ldx * n);
+  int nblk = ceil_div(n, NB);
+  trtri_diag_kernel<<<nblk, 256, 0, s>>>(n, L, ldl, X, ldx);
+  count_launch();
+  for (int b = 1; b < nblk; ++b) {
+    int i0 = b * NB, jb = std::min(NB, n - i0);
+    // T = L[i0:i0+jb, 0:i0] * X[0:i0, 0:i0]   (X lower)
+    dgemm(s, 'N', 'N', jb, i0, i0, 1.0, L + i0, ldl, X, ldx, 0.0, work, NB, kBLower);
+    // X[i0:, 0:i0] = -X_ii * T
+    dgemm(s, 'N', 'N', jb, i0, jb, -1.0, X + i0 + (size_t)i0 * ldx, ldx, work, NB, 0.0, X + i0, ldx,
+          kALower);
+  }
+}
+
+// ------------------------------------------------------------------------------------- sytrd
+// Blocked lower tridiagonalisation with panel width PB (Householder vectors explicit in V).
+constexpr int PB = 32;
+constexpr int ST = 64;        // symv tile
+constexpr int RED_THREADS = 1024;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NT>
+__device__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : 0.0;
+    r = warp_sum(r);
+    if (threadIdx.x == 0) sh[0] = r;
+  }
+  __syncthreads();
+  r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Step 1 of column j: apply the panel's previous reflectors to A(j:n, j), then generate the
+// reflector that annihilates A(j+2:n, j) (dlarfg semantics: beta = -sign(alpha) ||x||).
+__global__ void __launch_bounds__(RED_THREADS) latrd_column_kernel(
+    int n, int j, int jj, double *A, int lda, double *Vp, double *Wp, double *V, int ldv, double *d,
+    double *e, double *tau) {
+  __shared__ double sh[32];
+  __shared__ double coef[2 * PB];
+  const int t = threadIdx.x;
+  if (t < jj) {
+    coef[t] = Wp[j + (size_t)t * n];        // W(j, q)
+    coef[PB + t] = Vp[j + (size_t)t * n];   // V(j, q)
+  }
+  __syncthreads();
+  double *col = A + (size_t)j * lda;
+  double sig = 0.0;
+  for (int r = j + t; r < n; r += RED_THREADS) {
+    double a = col[r];
+    for (int q = 0; q < jj; ++q)
+      a -= Vp[r + (size_t)q * n] * coef[q] + Wp[r + (size_t)q * n] * coef[PB + q];
+    col[r] = a;
+    if (r >= j + 2) sig = fma(a, a, sig);
+  }
+  sig = block_sum<RED_THREADS>(sig, sh);
+  // col[j], col[j+1] were written by threads 0 and 1 (r = j, j+1); make them visible.
+  __syncthreads();
+  __shared__ double s_scale, s_beta, s_tau;
+  if (t == 0) {
+    double dj = col[j];
+    d[j] = dj;
+    if (j + 1 < n) {
+      double alpha = col[j + 1];
+      double beta, tv, scale;
+      if (sig == 0.0) {
+        tv = 0.0;
+        beta = alpha;
+        scale = 0.0;
+      } else {
+        beta = -copysign(sqrt(alpha * alpha + sig), alpha);
+        tv = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      e[j] = beta;
+      tau[j] = tv;
+      s_scale = scale;
+      s_beta = beta;
+      s_tau = tv;
+    }
+  }
+  __syncthreads();
+  if (j + 1 >= n) return;
+  double scale = s_scale;
+  for (int r = t; r < n; r += RED_THREADS) {
+    double v;
+    if (r <= j) v = 0.0;
+    else if (r == j + 1) v = 1.0;
+    else v = col[r] * scale;
+    Vp[r + (size_t)jj * n] = v;
+    V[r + (size_t)j * ldv] = v;
+  }
+}
+
+// y(j+1:n) = A22 v with A22 = A(j+1:n, j+1:n) read from its lower triangle only; partial sums per
+// 64x64 tile pair are reduced deterministically by symv_reduce_kernel.
+__global__ void __launch_bounds__(256) symv_partial_kernel(int m, int T, const double *A22, int lda,
+                                                           const double *v, double *P) {
+  __shared__ double tile[ST][ST + 1];
+  __shared__ double vr[ST], vc[ST];
+  // decode lower tile index -> (r, c), c <= r
+  int idx = blockIdx.x;
+  int r = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
+  while ((r + 1) * (r + 2) / 2 <= idx) ++r;
+  while (r * (r + 1) / 2 > idx) --r;
+  int c = idx - r * (r + 1) / 2;
+  const int t = threadIdx.x;
+  const int ri0 = r * ST, ci0 = c * ST;
+  for (int k = t; k < ST * ST; k += 256) {
+    int ii = k % ST, jj = k / ST;
+    int gi = ri0 + ii, gj = ci0 + jj;
+    double a = 0.0;
+    if (gi < m && gj < m) {
+      if (r == c && ii < jj) a = 0.0;  // filled by mirroring below
+      else a = A22[gi + (size_t)gj * lda];
+    }
+    tile[ii][jj] = a;
+  }
+  if (t < ST) {
+    vr[t] = (ri0 + t < m) ? v[ri0 + t] : 0.0;
+    vc[t] = (ci0 + t < m) ? v[ci0 + t] : 0.0;
+  }
+  __syncthreads();
+  if (r == c) {
+    for (int k = t; k < ST * ST; k += 256) {
+      int ii = k % ST, jj = k / ST;
+      if (ii < jj) tile[ii][jj] = tile[jj][ii];
+    }
+    __syncthreads();
+  }
+  // rows: 4 threads per row, each 16 columns
+  {
+    int row = t >> 2, part = t & 3;
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) s = fma(tile[row][part * 16 + q], vc[part * 16 + q], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (part == 0) P[((size_t)r * T + c) * ST + row] = s;
+  }
+  if (c < r) {
+    int colq = t >> 2, part = t & 3;
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) s = fma(tile[part * 16 + q][colq], vr[part * 16 + q], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (part == 0) P[((size_t)c * T + r) * ST + colq] = s;
+  }
+}
+
+__global__ void symv_reduce_kernel(int m, int T, const double *P, double *y) {
+  int r = blockIdx.x, i = threadIdx.x;
+  if (r * ST + i >= m) return;
+  double s = 0.0;
+  for (int c = 0; c < T; ++c) s += P[((size_t)r * T + c) * ST + i];
+  y[r * ST + i] = s;
+}
+
+// dots[q] = W(:,q)^T v, dots[PB+q] = V(:,q)^T v over rows j+1..n-1 (one CTA per dot).
+__global__ void latrd_dots_kernel(int n, int j, int jj, const double *Vp, const double *Wp, double *dots) {
+  __shared__ double sh[32];
+  int q = blockIdx.x % jj;
+  bool isV = blockIdx.x >= jj;
+  const double *X = (isV ? Vp : Wp) + (size_t)q * n;
+  const double *v = Vp + (size_t)jj * n;
+  double s = 0.0;
+  for (int r = j + 1 + threadIdx.x; r < n; r += 256) s = fma(X[r], v[r], s);
+  s = block_sum<256>(s, sh);
+  if (threadIdx.x == 0) dots[(isV ? PB : 0) + q] = s;
+}
+
+// w = tau (y - V (W^T v) - W (V^T v)); partial sums of w^T v per CTA.
+__global__ void latrd_w_kernel(int n, int j, int jj, const double *Vp, double *Wp, const double *y,
+                               const double *dots, const double *tau, double *part) {
+  __shared__ double sh[32];
+  __shared__ double cf[2 * PB];
+  if (threadIdx.x < jj) {
+    cf[threadIdx.x] = dots[threadIdx.x];
+    cf[PB + threadIdx.x] = dots[PB + threadIdx.x];
+  }
+  __syncthreads();
+  const double tv = tau[j];
+  const double *v = Vp + (size_t)jj * n;
+  double *w = Wp + (size_t)jj * n;
+  double s = 0.0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    double val = 0.0;
+    if (r > j) {
+      val = y[r];
+      for (int q = 0; q < jj; ++q)
+        val -= Vp[r + (size_t)q * n] * cf[q] + Wp[r + (size_t)q * n] * cf[PB + q];
+      val *= tv;
+      s = fma(val, v[r], s);
+    }
+    w[r] = val;
+  }
+  s = block_sum<256>(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void latrd_w2_kernel(int n, int j, int jj, const double *Vp, double *Wp, const double *tau,
+                                const double *part, int nparts) {
+  __shared__ double alpha;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += part[i];
+    alpha = -0.5 * tau[j] * s;
+  }
+  __syncthreads();
+  const double *v = Vp + (size_t)jj * n;
+  double *w = Wp + (size_t)jj * n;
+  double a = alpha;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    if (r > j) w[r] = fma(a, v[r], w[r]);
+}
+
+__global__ void copy_last_diag_kernel(int n, const double *A, int lda, double *d) {
+  d[n - 1] = A[(n - 1) + (size_t)(n - 1) * lda];
+}
+
+size_t sytrd_work_size(int n) {
+  size_t T = (size_t)ceil_div(n, ST);
+  return 2 * (size_t)n * PB + (size_t)n + T * T * ST + 2 * PB + 1024;
+}
+
+void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e, double *tau, double *V,
+                 int ldv, double *work) {
+  double *Vp = work;
+  double *Wp = Vp + (size_t)n * PB;
+  double *y = Wp + (size_t)n * PB;
+  double *P = y + n;
+  size_t T0 = (size_t)ceil_div(n, ST);
+  double *dots = P + T0 * T0 * ST;
+  double *part = dots + 2 * PB;
+  set_zero(s, V, (size_t)ldv * n);
+  if (n == 1) {
+    copy_last_diag_kernel<<<1, 1, 0, s>>>(n, A, lda, d);
+    count_launch();
+    return;
+  }
+  const int wblocks = std::min(ceil_div(n, 256), 64);
+  for (int p0 = 0; p0 < n - 1; p0 += PB) {
+    int nbp = std::min(PB, n - 1 - p0);
+    for (int jj = 0; jj < nbp; ++jj) {
+      int j = p0 + jj;
+      latrd_column_kernel<<<1, RED_THREADS, 0, s>>>(n, j, jj, A, lda, Vp, Wp, V, ldv, d, e, tau);
+      int m = n - j - 1;
+      int T = ceil_div(m, ST);
+      const double *A22 = A + (j + 1) + (size_t)(j + 1) * lda;
+      symv_partial_kernel<<<T * (T + 1) / 2, 256, 0, s>>>(m, T, A22, lda, Vp + (size_t)jj * n + j + 1, P);
+      symv_reduce_kernel<<<T, ST, 0, s>>>(m, T, P, y + j + 1);
+      count_launch(3);
+      if (jj > 0) {
+        latrd_dots_kernel<<<2 * jj, 256, 0, s>>>(n, j, jj, Vp, Wp, dots);
+        count_launch();
+      }
+      latrd_w_kernel<<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, y, dots, tau, part);
+      latrd_w2_kernel<<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, tau, part, wblocks);
+      count_launch(2);
+    }
+    int t0 = p0 + nbp;
+    int m2 = n - t0;
+    if (m2 > 0) {
+      double *At = A + t0 + (size_t)t0 * lda;
+      dgemm(s, 'N', 'T', m2, m2, nbp, -1.0, Vp + t0, n, Wp + t0, n, 1.0, At, lda, kCLower);
+      dgemm(s, 'N', 'T', m2, m2, nbp, -1.0, Wp + t0, n, Vp + t0, n, 1.0, At, lda, kCLower);
+    }
+  }
+  copy_last_diag_kernel<<<1, 1, 0, s>>>(n, A, lda, d);
+  count_launch();
+}
+
+// ------------------------------------------------------------------------------------- ormtr
+constexpr int OB = 64;
+
+// T (nb x nb, upper) of the compact WY form: H_p..H_{p+nb-1} = I - V T V^T, from G = V^T V.
+__global__ void larft_kernel(int nb, const double *G, const double *tau, double *T) {
+  __shared__ double t[OB][OB + 1];
+  const int tid = threadIdx.x;
+  for (int k = tid; k < OB * OB; k += blockDim.x) t[k % OB][k / OB] = 0.0;
+  __syncthreads();
+  for (int i = 0; i < nb; ++i) {
+    // t(0:i, i) = -tau_i * T(0:i, 0:i) * G(0:i, i)
+    double ti = tau[i];
+    double v = 0.0;
+    if (tid < i) {
+      for (int q = tid; q < i; ++q) v = fma(t[tid][q], G[q + (size_t)i * nb], v);
+      v *= -ti;
+    }
+    __syncthreads();
+    if (tid < i) t[tid][i] = v;
+    if (tid == 0) t[i][i] = ti;
+    __syncthreads();
+  }
+  for (int k = tid; k < nb * nb; k += blockDim.x) T[k] = t[k % nb][k / nb];
+}
+
+size_t ormtr_work_size(int n, int k) {
+  return 2 * (size_t)OB * OB + 2 * (size_t)OB * std::max(k, 1);
+}
+
+void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const double *tau, double *Z,
+                int ldz, double *work) {
+  if (n <= 1 || k <= 0) return;
+  double *G = work;
+  double *T = G + OB * OB;
+  double *M = T + OB * OB;
+  double *M2 = M + (size_t)OB * k;
+  int nref = n - 1;  // reflectors j = 0 .. n-2
+  int last = ((nref - 1) / OB) * OB;
+  for (int p0 = last; p0 >= 0; p0 -= OB) {
+    int nb = std::min(OB, nref - p0);
+    int r0 = p0 + 1;          // first nonzero row of the block's vectors
+    int mr = n - r0;
+    const double *Vb = V + r0 + (size_t)p0 * ldv;
+    dgemm(s, 'T', 'N', nb, nb, mr, 1.0, Vb, ldv, Vb, ldv, 0.0, G, nb);
+    larft_kernel<<<1, OB, 0, s>>>(nb, G, tau + p0, T);
+    count_launch();
+    dgemm(s, 'T', 'N', nb, k, mr, 1.0, Vb, ldv, Z + r0, ldz, 0.0, M, nb);
+    dgemm(s, 'N', 'N', nb, k, nb, 1.0, T, nb, M, nb, 0.0, M2, nb, kAUpper);
+    dgemm(s, 'N', 'N', mr, k, nb, -1.0, Vb, ldv, M2, nb, 1.0, Z + r0, ldz);
+  }
+}
+
+}  // namespace dg

@@ -1,0 +1,52 @@
+// FP64 dense linear algebra on one GB300 (column-major, device pointers, one stream).
+#pragma once
+#include "common.cuh"
+
+namespace dg {
+
+// Triangular structure hints for dgemm (zero regions are skipped, not read).
+enum GemmFlags : int {
+  kALower = 1,   // op(A)[i][p] == 0 for p > i
+  kAUpper = 2,   // op(A)[i][p] == 0 for p < i
+  kBLower = 4,   // op(B)[p][j] == 0 for p < j
+  kBUpper = 8,   // op(B)[p][j] == 0 for p > j
+  kCLower = 16,  // only tiles touching the lower triangle (i >= j) are computed
+};
+
+// C = alpha * op(A) * op(B) + beta * C ; op = 'N' or 'T'. m, n, k >= 0.
+void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
+           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0);
+
+// In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
+void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);
+
+// X = L^{-1} for lower-triangular L (X lower, strict upper zero). work: 64*n doubles.
+void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work);
+
+// Symmetric tridiagonal reduction A = Q T Q^T from the lower triangle of A (n x n, lda).
+// d[n], e[n-1], tau[n-1]; V (n x n, ldv) receives the Householder vectors explicitly
+// (column j: zeros for rows <= j, 1 at row j+1). work: see sytrd_work_size().
+size_t sytrd_work_size(int n);
+void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e, double *tau,
+                 double *V, int ldv, double *work);
+
+// Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: see ormtr_work_size().
+size_t ormtr_work_size(int n, int k);
+void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const double *tau, double *Z,
+                int ldz, double *work);
+
+// Symmetric tridiagonal eigensolver (divide and conquer): d[n] (in: diagonal, out: eigenvalues
+// ascending), e[n-1] off-diagonal (destroyed); Q (n x n, ldq) eigenvectors. work sizes below.
+size_t stedc_work_size(int n);
+size_t stedc_iwork_size(int n);
+int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, double *work,
+          int *iwork, int *status_dev);
+
+// Small helpers
+void set_zero(cudaStream_t s, double *p, size_t n);
+void copy_lower_to_upper(cudaStream_t s, int n, double *A, int lda);
+void zero_strict_upper(cudaStream_t s, int n, double *A, int lda);
+void scale_columns(cudaStream_t s, int m, int n, const double *A, int lda, const double *f,
+                   double *B, int ldb);
+
+}  // namespace dg

@@ -1,0 +1,578 @@
+// Symmetric tridiagonal eigensolver by level-synchronous divide and conquer (Cuppen's method with
+// Dongarra-Sorensen deflation and the Gu-Eisenstat recomputation of z for orthogonality).
+//
+// The tridiagonal is torn at every block boundary (T = diag(T1, T2) + |beta| u u^T, u = e_m-1 +
+// sign(beta) e_m), leaves are single elements, and each level merges pairs of neighbouring blocks:
+//   sort    : merge the two sorted eigenvalue lists, form z = [Q1(last,:), sign Q2(first,:)] / sqrt2
+//   deflate : small |z| or close eigenvalue pairs (Givens rotation of the two Q columns)
+//   secular : 1 + rho sum w_j^2 / (d_j - lambda) = 0, one warp per root, bracketed two-pole
+//             rational iteration with bisection safeguard (bounded iterations, status on cap)
+//   zhat    : z_j^2 = prod_i (lambda_i - d_j) / (rho prod_{i != j} (d_i - d_j))
+//   vectors : U(:, i) = zhat / (d - lambda_i), normalised; Q_new = Q_nondeflated * U (GEMM)
+//   scatter : final ascending order of roots and deflated values, columns placed accordingly.
+// This replaces the tridiagonal stage of dsygvd (math/eigensolver.F90:561-660 'D' solvers).
+#include <algorithm>
+#include <vector>
+
+#include "linalg.cuh"
+
+namespace dg {
+
+constexpr double kEps = 2.220446049250313e-16;
+constexpr int kSecularMaxIter = 100;
+constexpr int kSmallMerge = 128;   // merges up to this size use the batched in-CTA product
+
+struct Merge {
+  int a, m, b;   // left block [a, m), right block [m, b); m == b means pass-through
+  int pad;
+};
+
+struct DcWork {
+  double *Ds, *zs, *dl, *w, *tau, *lam, *zh, *rot_cs, *vals;
+  int *perm, *ndpos, *dfpos, *org, *rot_cols, *mK, *mRot, *srcinfo;
+  double *Gs, *U, *Qtmp, *Qalt;
+};
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double wmax(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Tear: d[m-1] -= |e[m-1]|, d[m] -= |e[m-1]| for every block boundary m; leaves Q = I.
+__global__ void dc_tear_kernel(int n, double *d, const double *e, const int *bounds, int nb) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  int m = bounds[k];
+  double b = fabs(e[m - 1]);
+  d[m - 1] -= b;
+  d[m] -= b;
+}
+
+__global__ void dc_identity_kernel(int n, double *Q, int ldq) {
+  int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    Q[i + (size_t)j * ldq] = (i == j) ? 1.0 : 0.0;
+}
+
+// K1: merge-sort the two eigenvalue lists and form z.
+__global__ void dc_sort_kernel(const Merge *merges, const double *d, const double *e, const double *Q,
+                               int ldq, DcWork W) {
+  Merge mg = merges[blockIdx.x];
+  if (mg.m == mg.b) return;
+  const int a = mg.a, m = mg.m, b = mg.b;
+  const int nL = m - a, nR = b - m;
+  const double sgn = (e[m - 1] >= 0.0) ? 1.0 : -1.0;
+  const double is2 = 0.70710678118654752440;
+  for (int i = threadIdx.x; i < nL + nR; i += blockDim.x) {
+    double val, zv;
+    int pos, blk;
+    if (i < nL) {
+      val = d[a + i];
+      zv = Q[(m - 1) + (size_t)(a + i) * ldq] * is2;
+      int lo = 0, hi = nR;  // count right elements < val
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (d[m + mid] < val) lo = mid + 1; else hi = mid;
+      }
+      pos = i + lo;
+      blk = i;
+    } else {
+      int r = i - nL;
+      val = d[m + r];
+      zv = sgn * Q[m + (size_t)(m + r) * ldq] * is2;
+      int lo = 0, hi = nL;  // count left elements <= val
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (d[a + mid] <= val) lo = mid + 1; else hi = mid;
+      }
+      pos = r + lo;
+      blk = nL + r;
+    }
+    W.Ds[a + pos] = val;
+    W.zs[a + pos] = zv;
+    W.perm[a + pos] = blk;
+  }
+}
+
+// K2: deflation (sequential scan by one thread after a parallel max reduction).
+__global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W) {
+  const int mi = blockIdx.x;
+  Merge mg = merges[mi];
+  if (mg.m == mg.b) {
+    if (threadIdx.x == 0) { W.mK[mi] = 0; W.mRot[mi] = 0; }
+    return;
+  }
+  const int a = mg.a, N = mg.b - mg.a;
+  __shared__ double smax[2][32];
+  double md = 0.0, mz = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    md = fmax(md, fabs(W.Ds[a + i]));
+    mz = fmax(mz, fabs(W.zs[a + i]));
+  }
+  md = wmax(md);
+  mz = wmax(mz);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { smax[0][wid] = md; smax[1][wid] = mz; }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+    md = fmax(md, smax[0][k]);
+    mz = fmax(mz, smax[1][k]);
+  }
+  md = fmax(md, smax[0][0]);
+  mz = fmax(mz, smax[1][0]);
+  const double rho2 = 2.0 * fabs(e[mg.m - 1]);
+  const double tol = 8.0 * kEps * fmax(md, mz);
+  double *Ds = W.Ds + a, *zs = W.zs + a;
+  int *perm = W.perm + a;
+  int nrot = 0, K = 0, nD = 0;
+  // flags are kept in ndpos temporarily: 1 = deflated
+  int *flag = W.dfpos + a;
+  for (int j = 0; j < N; ++j) flag[j] = 0;
+  if (rho2 * mz <= tol) {
+    for (int j = 0; j < N; ++j) flag[j] = 1;
+  } else {
+    int prev = -1;
+    for (int j = 0; j < N; ++j) {
+      if (rho2 * fabs(zs[j]) <= tol) {
+        flag[j] = 1;
+        continue;
+      }
+      if (prev >= 0) {
+        double s = zs[prev], c = zs[j];
+        double t = hypot(c, s);
+        double tdiff = Ds[j] - Ds[prev];
+        c /= t;
+        s = -s / t;
+        if (fabs(tdiff * c * s) <= tol) {
+          zs[j] = t;
+          zs[prev] = 0.0;
+          W.rot_cols[2 * (a + nrot)] = a + perm[prev];
+          W.rot_cols[2 * (a + nrot) + 1] = a + perm[j];
+          W.rot_cs[2 * (a + nrot)] = c;
+          W.rot_cs[2 * (a + nrot) + 1] = s;
+          ++nrot;
+          double tt = Ds[prev] * c * c + Ds[j] * s * s;
+          Ds[j] = Ds[prev] * s * s + Ds[j] * c * c;
+          Ds[prev] = tt;
+          flag[prev] = 1;
+        }
+      }
+      prev = j;
+    }
+  }
+  // compact: non-deflated positions -> ndpos, deflated -> dfpos (overwrites the flags in order,
+  // safe because dfpos[t] is written only after flag[j] with j >= t has been read)
+  for (int j = 0; j < N; ++j) {
+    if (!flag[j]) {
+      W.ndpos[a + K] = j;
+      W.dl[a + K] = Ds[j];
+      W.w[a + K] = zs[j];
+      ++K;
+    } else {
+      flag[nD] = j;
+      ++nD;
+    }
+  }
+  W.mK[mi] = K;
+  W.mRot[mi] = nrot;
+}
+
+// K3: apply the recorded rotations to the Q columns (each thread owns a row of the block).
+__global__ void dc_rotate_kernel(const Merge *merges, double *Q, int ldq, DcWork W) {
+  const int mi = blockIdx.x;
+  Merge mg = merges[mi];
+  if (mg.m == mg.b) return;
+  const int nrot = W.mRot[mi];
+  if (nrot == 0) return;
+  int row = mg.a + blockIdx.y * blockDim.x + threadIdx.x;
+  if (row >= mg.b) return;
+  for (int k = 0; k < nrot; ++k) {
+    int cp = W.rot_cols[2 * (mg.a + k)], cj = W.rot_cols[2 * (mg.a + k) + 1];
+    double c = W.rot_cs[2 * (mg.a + k)], s = W.rot_cs[2 * (mg.a + k) + 1];
+    double x = Q[row + (size_t)cp * ldq], y = Q[row + (size_t)cj * ldq];
+    Q[row + (size_t)cp * ldq] = c * x + s * y;
+    Q[row + (size_t)cj * ldq] = c * y - s * x;
+  }
+}
+
+// K4: secular equation, one warp per root.
+__global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_merge, const double *e,
+                                  DcWork W, int *status) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= n) return;
+  const int mi = pos_merge[g];
+  if (mi < 0) return;
+  Merge mg = merges[mi];
+  const int a = mg.a;
+  const int K = W.mK[mi];
+  const int i = g - a;
+  if (i >= K) return;
+  const double rho = 2.0 * fabs(e[mg.m - 1]);
+  const double *dl = W.dl + a, *w = W.w + a;
+  int org;
+  double lo, hi, tau;
+  if (i < K - 1) {
+    double mid = 0.5 * (dl[i + 1] - dl[i]);
+    double s = 0.0;
+    for (int j = lane; j < K; j += 32) s += w[j] * w[j] / ((dl[j] - dl[i]) - mid);
+    double f = 1.0 + rho * wsum(s);
+    if (f > 0.0) { org = i; lo = 0.0; hi = mid; }
+    else { org = i + 1; lo = -mid; hi = 0.0; }
+  } else {
+    double s = 0.0;
+    for (int j = lane; j < K; j += 32) s += w[j] * w[j];
+    org = K - 1;
+    lo = 0.0;
+    hi = rho * wsum(s);
+  }
+  tau = 0.5 * (lo + hi);
+  const double dorg = dl[org];
+  bool conv = false;
+  for (int it = 0; it < kSecularMaxIter; ++it) {
+    double sf = 0.0, sp = 0.0, sq = 0.0;
+    for (int j = lane; j < K; j += 32) {
+      double dd = (dl[j] - dorg) - tau;
+      double t = w[j] * w[j] / dd;
+      sf += t;
+      if (j <= i) sp += t / dd; else sq += t / dd;
+    }
+    double f = 1.0 + rho * wsum(sf);
+    double psip = rho * wsum(sp);
+    double phip = rho * wsum(sq);
+    if (f > 0.0) hi = tau; else lo = tau;
+    if (f == 0.0) { conv = true; break; }
+    double nt;
+    if (i < K - 1) {
+      double dlo = (dl[i] - dorg) - tau, dhi = (dl[i + 1] - dorg) - tau;
+      double A = psip * dlo * dlo, B = phip * dhi * dhi;
+      double c = f - A / dlo - B / dhi;
+      double A2 = c, B2 = -(c * (dlo + dhi) + A + B), C2 = c * dlo * dhi + A * dhi + B * dlo;
+      double st;
+      if (A2 == 0.0) {
+        st = (B2 != 0.0) ? -C2 / B2 : 0.0;
+      } else {
+        double disc = sqrt(fmax(B2 * B2 - 4.0 * A2 * C2, 0.0));
+        double s1, s2;
+        if (B2 <= 0.0) {
+          double den = -B2 + disc;
+          s1 = den / (2.0 * A2);
+          s2 = (den != 0.0) ? 2.0 * C2 / den : s1;
+        } else {
+          double den = -B2 - disc;
+          s1 = den / (2.0 * A2);
+          s2 = 2.0 * C2 / den;
+        }
+        st = (s2 > dlo && s2 < dhi) ? s2 : s1;
+      }
+      nt = tau + st;
+    } else {
+      double dlo = (dl[K - 1] - dorg) - tau;
+      double A = psip * dlo * dlo;
+      double c = f - A / dlo;
+      nt = tau + ((c != 0.0) ? dlo + A / c : 0.0);
+    }
+    if (!(nt > lo && nt < hi)) nt = 0.5 * (lo + hi);
+    if (nt == tau || fabs(hi - lo) <= 2.0 * kEps * fmax(fabs(lo), fabs(hi))) {
+      tau = nt;
+      conv = true;
+      break;
+    }
+    tau = nt;
+  }
+  if (lane == 0) {
+    if (!conv) atomicExch(status, kDevIterCap);
+    W.org[a + i] = org;
+    W.tau[a + i] = tau;
+    W.lam[a + i] = dorg + tau;
+  }
+}
+
+// K5: Gu-Eisenstat zhat, one warp per j; product of O(1) ratios with exponent tracking.
+__global__ void dc_zhat_kernel(int n, const Merge *merges, const int *pos_merge, const double *e, DcWork W) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= n) return;
+  const int mi = pos_merge[g];
+  if (mi < 0) return;
+  Merge mg = merges[mi];
+  const int a = mg.a;
+  const int K = W.mK[mi];
+  const int j = g - a;
+  if (j >= K) return;
+  const double rho = 2.0 * fabs(e[mg.m - 1]);
+  const double *dl = W.dl + a;
+  const double dj = dl[j];
+  double p = 1.0;
+  int ex = 0;
+  for (int i = lane; i < K; i += 32) {
+    double num = (dl[W.org[a + i]] - dj) + W.tau[a + i];
+    double r = (i == j) ? num / rho : num / (dl[i] - dj);
+    p *= r;
+    double ap = fabs(p);
+    if (ap > 1e150 || (ap < 1e-150 && ap > 0.0)) {
+      int k;
+      p = frexp(p, &k);
+      ex += k;
+    }
+  }
+  // combine lane products
+  for (int o = 16; o > 0; o >>= 1) {
+    double po = __shfl_xor_sync(0xffffffffu, p, o);
+    int eo = __shfl_xor_sync(0xffffffffu, ex, o);
+    p *= po;
+    ex += eo;
+    int k;
+    p = frexp(p, &k);
+    ex += k;
+  }
+  if (lane == 0) {
+    double val = ldexp(p, ex);
+    double z = sqrt(fmax(val, 0.0));
+    W.zh[a + j] = copysign(z, W.w[a + j]);
+  }
+}
+
+// K6: eigenvector matrix of the rank-one problem, one warp per column i; U rows [0,K) at column a+i.
+__global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_merge, DcWork W, int ldu) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= n) return;
+  const int mi = pos_merge[g];
+  if (mi < 0) return;
+  Merge mg = merges[mi];
+  const int a = mg.a;
+  const int K = W.mK[mi];
+  const int i = g - a;
+  if (i >= K) return;
+  const double *dl = W.dl + a;
+  const double dorg = dl[W.org[a + i]];
+  const double tau = W.tau[a + i];
+  double *u = W.U + (size_t)(a + i) * ldu;
+  double s = 0.0;
+  for (int t = lane; t < K; t += 32) {
+    double v = W.zh[a + t] / ((dl[t] - dorg) - tau);
+    u[t] = v;
+    s += v * v;
+  }
+  double inv = 1.0 / sqrt(wsum(s));
+  for (int t = lane; t < K; t += 32) u[t] *= inv;
+}
+
+// K7: gather the non-deflated Q columns (rows [a,b)) into Gs at columns a .. a+K-1.
+__global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merge, const double *Q, int ldq,
+                                 DcWork W, int ldg) {
+  const int g = blockIdx.x;
+  const int mi = pos_merge[g];
+  if (mi < 0) return;
+  Merge mg = merges[mi];
+  const int a = mg.a;
+  const int K = W.mK[mi];
+  const int t = g - a;
+  if (t >= K) return;
+  int src = a + W.perm[a + W.ndpos[a + t]];
+  for (int r = mg.a + threadIdx.x; r < mg.b; r += blockDim.x)
+    W.Gs[r + (size_t)g * ldg] = Q[r + (size_t)src * ldq];
+}
+
+// K8 (small merges): Qtmp[a:b, a:a+K] = Gs[a:b, a:a+K] * U[0:K, a:a+K] inside one CTA.
+__global__ void dc_small_gemm_kernel(const Merge *merges, DcWork W, int ld) {
+  Merge mg = merges[blockIdx.x];
+  if (mg.m == mg.b) return;
+  const int K = W.mK[blockIdx.x];
+  const int a = mg.a, N = mg.b - mg.a;
+  for (int idx = threadIdx.x; idx < N * K; idx += blockDim.x) {
+    int r = idx % N, c = idx / N;
+    double s = 0.0;
+    const double *g = W.Gs + (a + r) + (size_t)a * ld;
+    const double *u = W.U + (size_t)(a + c) * ld;
+    for (int t = 0; t < K; ++t) s = fma(g[(size_t)t * ld], u[t], s);
+    W.Qtmp[(a + r) + (size_t)(a + c) * ld] = s;
+  }
+}
+
+// K9: final ascending order (rank in the union of roots and deflated values, ties by index).
+__global__ void dc_rank_kernel(const Merge *merges, double *d, DcWork W) {
+  const int mi = blockIdx.x;
+  Merge mg = merges[mi];
+  const int a = mg.a, N = mg.b - mg.a;
+  int e0 = blockIdx.y * blockDim.x + threadIdx.x;
+  if (e0 >= N) return;
+  if (mg.m == mg.b) {  // pass-through block: identity mapping
+    W.srcinfo[a + e0] = a + e0;
+    W.vals[a + e0] = d[a + e0];
+    return;
+  }
+  const int K = W.mK[mi];
+  auto value = [&](int k) -> double {
+    return (k < K) ? W.lam[a + k] : W.Ds[a + W.dfpos[a + (k - K)]];
+  };
+  double v = value(e0);
+  int rank = 0;
+  for (int k = 0; k < N; ++k) {
+    double u = value(k);
+    if (u < v || (u == v && k < e0)) ++rank;
+  }
+  W.vals[a + rank] = v;
+  // source column: >= 0 -> column of Q (deflated); < 0 -> -(1 + column of Qtmp)
+  W.srcinfo[a + rank] = (e0 < K) ? -(1 + a + e0) : (a + W.perm[a + W.dfpos[a + (e0 - K)]]);
+}
+
+// K10: scatter the columns into the output buffer and the values into d.
+__global__ void dc_scatter_kernel(int n, const int *pos_merge_all, const Merge *merges, const double *Q,
+                                  int ldq, double *Qout, double *d, DcWork W, int ldt) {
+  const int g = blockIdx.x;
+  const int mi = pos_merge_all[g];
+  Merge mg = merges[mi];
+  int src = W.srcinfo[g];
+  const double *col = (src >= 0) ? Q + (size_t)src * ldq : W.Qtmp + (size_t)(-src - 1) * ldt;
+  for (int r = mg.a + threadIdx.x; r < mg.b; r += blockDim.x) Qout[r + (size_t)g * ldq] = col[r];
+  if (threadIdx.x == 0) d[g] = W.vals[g];
+}
+
+// ------------------------------------------------------------------------------------- host side
+struct DcLevel {
+  std::vector<Merge> merges;
+  std::vector<int> pos_merge;      // merge index for positions inside real merges, -1 otherwise
+  std::vector<int> pos_merge_all;  // merge index (including pass-through) for every position
+  int max_block = 0;
+};
+
+static std::vector<DcLevel> plan_levels(int n, std::vector<int> &bounds) {
+  std::vector<std::pair<int, int>> cur;
+  for (int i = 0; i < n; ++i) cur.push_back({i, i + 1});
+  std::vector<DcLevel> levels;
+  while (cur.size() > 1) {
+    DcLevel L;
+    std::vector<std::pair<int, int>> nxt;
+    for (size_t k = 0; k < cur.size(); k += 2) {
+      if (k + 1 < cur.size()) {
+        L.merges.push_back({cur[k].first, cur[k].second, cur[k + 1].second, 0});
+        bounds.push_back(cur[k].second);
+        nxt.push_back({cur[k].first, cur[k + 1].second});
+      } else {
+        L.merges.push_back({cur[k].first, cur[k].second, cur[k].second, 0});
+        nxt.push_back(cur[k]);
+      }
+    }
+    L.pos_merge.assign(n, -1);
+    L.pos_merge_all.assign(n, -1);
+    for (size_t mi = 0; mi < L.merges.size(); ++mi) {
+      const Merge &mg = L.merges[mi];
+      for (int p = mg.a; p < mg.b; ++p) {
+        L.pos_merge_all[p] = (int)mi;
+        if (mg.m != mg.b) L.pos_merge[p] = (int)mi;
+      }
+      L.max_block = std::max(L.max_block, mg.b - mg.a);
+    }
+    levels.push_back(std::move(L));
+    cur.swap(nxt);
+  }
+  return levels;
+}
+
+size_t stedc_work_size(int n) {
+  // 9 vectors of n, rotations (2n), 4 matrices n x n
+  return (size_t)n * 9 + 2 * (size_t)n + 4 * (size_t)n * n + 64;
+}
+size_t stedc_iwork_size(int n) {
+  int levels = 0;
+  while ((1LL << levels) < n) ++levels;
+  // 10 n index vectors + plan metadata (bounds n, merges 4 n, two position maps per level)
+  return (size_t)n * (10 + 1 + 4 + 2 * (size_t)(levels + 1)) + 64;
+}
+
+int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, double *work, int *iwork,
+          int *status_dev) {
+  if (n <= 0) return 0;
+  if (ldq != n) return -1;  // the workspace layout assumes a square, tightly packed Q
+  dim3 gi(ceil_div(n, 256), n);
+  dc_identity_kernel<<<gi, 256, 0, s>>>(n, Q, ldq);
+  count_launch();
+  if (n == 1) return 0;
+  std::vector<int> bounds;
+  std::vector<DcLevel> levels = plan_levels(n, bounds);
+
+  DcWork W;
+  double *p = work;
+  W.Ds = p; p += n; W.zs = p; p += n; W.dl = p; p += n; W.w = p; p += n; W.tau = p; p += n;
+  W.lam = p; p += n; W.zh = p; p += n; W.vals = p; p += n; p += n;
+  W.rot_cs = p; p += 2 * (size_t)n;
+  W.Gs = p; p += (size_t)n * n; W.U = p; p += (size_t)n * n; W.Qtmp = p; p += (size_t)n * n;
+  W.Qalt = p; p += (size_t)n * n;
+  int *ip = iwork;
+  W.perm = ip; ip += n; W.ndpos = ip; ip += n; W.dfpos = ip; ip += n; W.org = ip; ip += n;
+  W.srcinfo = ip; ip += n; W.mK = ip; ip += n; W.mRot = ip; ip += n; ip += n;
+  W.rot_cols = ip; ip += 2 * (size_t)n;
+  int *dev_meta = ip;  // bounds + per-level merges and position maps (uploaded below)
+
+  // upload the plan: bounds, then per level (merges, pos_merge, pos_merge_all)
+  std::vector<int> meta(bounds.begin(), bounds.end());
+  std::vector<size_t> off_merge, off_pm, off_pma;
+  for (auto &L : levels) {
+    off_merge.push_back(meta.size());
+    for (auto &mg : L.merges) { meta.push_back(mg.a); meta.push_back(mg.m); meta.push_back(mg.b); meta.push_back(0); }
+    off_pm.push_back(meta.size());
+    meta.insert(meta.end(), L.pos_merge.begin(), L.pos_merge.end());
+    off_pma.push_back(meta.size());
+    meta.insert(meta.end(), L.pos_merge_all.begin(), L.pos_merge_all.end());
+  }
+  // the metadata lives in a dedicated device allocation owned by the caller's iwork tail
+  cudaMemcpyAsync(dev_meta, meta.data(), meta.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+
+  dc_tear_kernel<<<ceil_div((int)bounds.size(), 256), 256, 0, s>>>(n, d, e, dev_meta, (int)bounds.size());
+  count_launch();
+
+  double *Qin = Q, *Qout = W.Qalt;
+  std::vector<int> hK;
+  for (size_t li = 0; li < levels.size(); ++li) {
+    DcLevel &L = levels[li];
+    const Merge *dm = reinterpret_cast<const Merge *>(dev_meta + off_merge[li]);
+    const int *pm = dev_meta + off_pm[li];
+    const int *pma = dev_meta + off_pma[li];
+    int nm = (int)L.merges.size();
+    dc_sort_kernel<<<nm, 256, 0, s>>>(dm, d, e, Qin, ldq, W);
+    dc_deflate_kernel<<<nm, 256, 0, s>>>(dm, e, W);
+    dim3 gr(nm, ceil_div(L.max_block, 256));
+    dc_rotate_kernel<<<gr, 256, 0, s>>>(dm, Qin, ldq, W);
+    int warps_blocks = ceil_div((long long)n * 32, 256);
+    dc_secular_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W, status_dev);
+    dc_zhat_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W);
+    dc_build_u_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, W, n);
+    dc_gather_kernel<<<n, 128, 0, s>>>(n, dm, pm, Qin, ldq, W, n);
+    count_launch(7);
+    if (L.max_block <= kSmallMerge) {
+      dc_small_gemm_kernel<<<nm, 256, 0, s>>>(dm, W, n);
+      count_launch();
+    } else {
+      hK.resize(nm);
+      cudaMemcpyAsync(hK.data(), W.mK, nm * sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      for (int k = 0; k < nm; ++k) {
+        const Merge &mg = L.merges[k];
+        if (mg.m == mg.b || hK[k] == 0) continue;
+        int a = mg.a, N = mg.b - mg.a, K = hK[k];
+        dgemm(s, 'N', 'N', N, K, K, 1.0, W.Gs + a + (size_t)a * n, n, W.U + (size_t)a * n, n, 0.0,
+              W.Qtmp + a + (size_t)a * n, n);
+      }
+    }
+    dim3 grk(nm, ceil_div(L.max_block, 256));
+    dc_rank_kernel<<<grk, 256, 0, s>>>(dm, d, W);
+    dc_scatter_kernel<<<n, 128, 0, s>>>(n, pma, dm, Qin, ldq, Qout, d, W, n);
+    count_launch(2);
+    std::swap(Qin, Qout);
+  }
+  if (Qin != Q) {
+    cudaMemcpyAsync(Q, Qin, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
+  }
+  return 0;
+}
+
+}  // namespace dg

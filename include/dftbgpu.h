@@ -1,0 +1,143 @@
+/*
+ * dftbgpu: GB300-native SCC-DFTB hot path (non-periodic Gamma point: SCC cycle, energy, forces).
+ *
+ * Plain C-ABI (no C++ or torch types) so that the reference's Fortran host can bind it with
+ * iso_c_binding, exactly as it binds MAGMA through extlibs/magma.F90:30-60 over
+ * extlibs/magmac.c:24-46. All arrays are caller-owned host memory unless a name ends in _dev.
+ * Units are atomic (Bohr, Hartree). Matrices are column-major. Every call returns 0 on success or
+ * one of the DFTBGPU_ERR_* codes below; dftbgpu_last_error() gives the message.
+ *
+ * Which reference call each entry point replaces is stated beside it (paths relative to
+ * src/dftbp/ of DFTB+ 25.1).
+ */
+#ifndef DFTBGPU_H
+#define DFTBGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DFTBGPU_OK = 0,
+  DFTBGPU_ERR_ARGS = 1,              /* invalid argument / size */
+  DFTBGPU_ERR_CUDA = 2,              /* CUDA runtime error */
+  DFTBGPU_ERR_NOT_POSDEF = 3,        /* overlap matrix not positive definite (cf. eigensolver.F90:1232) */
+  DFTBGPU_ERR_SCC_NOT_CONVERGED = 4, /* SCC not converged and convergent_only set (main.F90:1679-1690) */
+  DFTBGPU_ERR_FERMI = 5,             /* Fermi level search failed (dftb/etemp.F90:179) */
+  DFTBGPU_ERR_ITER_CAP = 6,          /* a bounded device iteration hit its cap (eigensolver) */
+  DFTBGPU_ERR_STATE = 7,             /* call order violated (e.g. forces before scc) */
+  DFTBGPU_ERR_NO_DEVICE = 8
+};
+
+/* Precision forms of the SCC cycle. */
+enum {
+  DFTBGPU_PREC_FP64 = 0,   /* plain FP64 drop-in */
+  DFTBGPU_PREC_MIXED = 1   /* reduced-precision early iterations, FP64-refined final iteration */
+};
+
+typedef struct dftbgpu_ctx dftbgpu_ctx;
+
+/* SCC options; field meaning as in the HSD input the reference parses (dftbplus/parser.F90). */
+typedef struct {
+  double kT;              /* Filling = Fermi { Temperature } (Ha) */
+  double scc_tol;         /* SCCTolerance: max |q_out - q_in| per mixed charge (e) */
+  int max_iter;           /* MaxSCCIterations */
+  int min_iter;           /* MinSCCIterations (default 1) */
+  double mix_alpha;       /* Broyden MixingParameter (0.2) */
+  double mix_omega0;      /* InverseJacobiWeight (0.01) */
+  double mix_min_weight;  /* MinimalWeight (1.0) */
+  double mix_max_weight;  /* MaximalWeight (1e5) */
+  double mix_weight_fac;  /* WeightFactor (1e-2) */
+  double net_charge;      /* Charge (e); N_el = sum(reference occupations) - net_charge */
+  int precision;          /* DFTBGPU_PREC_* */
+  int convergent_only;    /* ConvergentSCCOnly: return DFTBGPU_ERR_SCC_NOT_CONVERGED if 1 */
+} dftbgpu_scc_opts;
+
+/* Energy terms as in dftb/energytypes.F90 (TEnergies) for this path. */
+typedef struct {
+  double EnonSCC, Escc, Erep, Eband, TS, E0, Etotal, EMermin;
+} dftbgpu_energies;
+
+/* Fill opts with the reference's defaults (parser.F90:5786-5790, Fermi kT = 0). */
+void dftbgpu_default_opts(dftbgpu_scc_opts *opts);
+
+/* Context lifecycle: one GPU, one stream per context. Replaces the MAGMA bring-up
+ * extlibs/magmac.c:24-46 (dftbp_extlibs_magma_get_gpus_available) / common/gpuenv.F90. */
+int dftbgpu_create(dftbgpu_ctx **ctx, int device);
+int dftbgpu_destroy(dftbgpu_ctx *ctx);
+const char *dftbgpu_last_error(const dftbgpu_ctx *ctx);
+
+/*
+ * Species data and Slater-Koster tables, uploaded once. Replaces the device-side use of the
+ * containers built by readSKFiles (dftbplus/parser.F90:3668-3886) + getFullTable (:4061-4130).
+ *   n_shell[nsp], ang_shell[4*nsp] (row-major [sp][shell]), onsite[4*nsp], ref_occ[4*nsp],
+ *   hubbu[nsp] (one U per species: non-orbital-resolved SCC).
+ *   Ordered pair p = sp1*nsp + sp2: sk_dist[p] grid spacing, sk_rows[p] rows (row j <-> r=(j+1)*dist),
+ *   sk_nint[p] integrals; sk_ham/sk_over concatenated over p, each pair column-major (rows fastest).
+ *   rep_nspline[p]; rep_data concatenated over p, each [cutoff, a1, a2, a3, x_start[nS],
+ *   cubic coeffs 4*(nS-1), last coeffs 6] (dftb/repulsive/splinerep.F90).
+ */
+int dftbgpu_set_model(dftbgpu_ctx *ctx, int nsp, const int *n_shell, const int *ang_shell,
+                      const double *onsite, const double *hubbu, const double *ref_occ,
+                      const double *sk_dist, const int *sk_rows, const int *sk_nint,
+                      const double *sk_ham, const double *sk_over,
+                      const int *rep_nspline, const double *rep_data);
+
+/*
+ * Geometry: coords[3*nAtom] (x,y,z per atom, Bohr), species[nAtom] (0-based). The GPU builds the
+ * cluster half neighbour list itself (same pairs as dftb/periodic.F90:380-700 for a non-periodic
+ * system), then H0 and S (buildH0/buildS, dftb/nonscc.F90:66-181) and the Cholesky factor of S.
+ * Replaces the H0/S part of processGeometry (dftbplus/main.F90:1219-1222).
+ */
+int dftbgpu_set_geometry(dftbgpu_ctx *ctx, int natom, const double *coords, const int *species);
+/* Same with device pointers (coords_dev[3*natom], species_dev[natom]); species must also be given
+ * on the host (species_host) because the orbital layout is host metadata. */
+int dftbgpu_set_geometry_dev(dftbgpu_ctx *ctx, int natom, const double *coords_dev,
+                             const int *species_host);
+
+/*
+ * SCC cycle to convergence: potentials, H = H0 + 1/2 S(V+V), generalized eigensolve, Fermi filling,
+ * density matrix, Mulliken, energies, Broyden mixing (dftbplus/main.F90:1429-1563 with
+ * hamiltonian.F90:148-450, eigenvects.F90:57-102, etemp.F90:59-191, densitymatrix.F90:530-591,
+ * populations.F90:120-191, getenergies.F90:47-384, mixer/broydenmixer.F90:180-342).
+ *   q_init[natom]: initial atomic populations or NULL for the neutral reference (q0).
+ *   Outputs (each may be NULL): energies, ef, eigen[nOrb], filling[nOrb] (x2 spin), q_out[natom]
+ *   (Mulliken populations per atom), n_iter, converged.
+ */
+int dftbgpu_scc(dftbgpu_ctx *ctx, const dftbgpu_scc_opts *opts, const double *q_init,
+                dftbgpu_energies *energies, double *ef, double *eigen, double *filling,
+                double *q_out, int *n_iter, int *converged);
+
+/*
+ * Energy gradient (not forces) of the converged state, grad[3*natom] (x,y,z per atom).
+ * Energy-weighted density matrix + derivative_blockEuclidean (dftb/forces.F90:548-669, FD SK
+ * derivatives nonscc.F90:428-484) + SCC double-counting (scc.F90:794-843) + repulsive
+ * (repulsive/twobodyrep.F90:273-332). Replaces main.F90:1777-1800.
+ */
+int dftbgpu_gradients(dftbgpu_ctx *ctx, double *grad);
+int dftbgpu_gradients_dev(dftbgpu_ctx *ctx, double *grad_dev);
+
+/* Sizes and per-orbital Mulliken populations of the converged state (qOutput, mOrb x nAtom
+ * collapsed to the nOrb orbitals in atom order). */
+int dftbgpu_n_orbitals(const dftbgpu_ctx *ctx, int *n_orb);
+int dftbgpu_get_orbital_populations(dftbgpu_ctx *ctx, double *q_orb);
+
+/*
+ * Dense generalized symmetric-definite eigensolver on the GPU: A x = lambda B x, all pairs,
+ * eigenvalues ascending. Replaces hegvd / magmaHegvd (math/eigensolver.F90:561-660, :1143-1245):
+ * A is overwritten by the eigenvectors (B-orthonormal columns), B by its Cholesky factor (lower).
+ * n x n column-major host arrays.
+ */
+int dftbgpu_sygvd(dftbgpu_ctx *ctx, int n, double *a, double *b, double *w);
+
+/* Debug/inspection of device state for tests: which = 0 H0, 1 S, 2 rho (density matrix),
+ * 3 H (last SCC Hamiltonian), 4 W (energy-weighted DM; valid after gradients). out[nOrb*nOrb]. */
+int dftbgpu_get_matrix(dftbgpu_ctx *ctx, int which, double *out);
+
+/* Number of this library's kernel launches since creation (for launch accounting). */
+long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DFTBGPU_H */
