@@ -61,7 +61,16 @@ SIGNATURES = {
     "dftbgpu_sygvd": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_get_matrix": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "dftbgpu_kernel_launches": (C.c_longlong, [C.c_void_p]),
+    "dftbgpu_test_dgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_double,
+                                     _dp, _dp, C.c_double, _dp, C.c_int]),
+    "dftbgpu_test_tridiag": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
+    "dftbgpu_test_stedc": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
+    "dftbgpu_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
+    "dftbgpu_profile_read": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_longlong)]),
 }
+
+PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
+          "density", "mulliken_energy", "broyden", "gradients", "gemm_fp64"]
 
 _lib = None
 
@@ -179,8 +188,61 @@ class Context:
         self.check(self.lib.dftbgpu_sygvd(self.h, n, _p(A, C.c_double), _p(B, C.c_double), _p(w, C.c_double)))
         return w, A, B
 
+    def test_dgemm(self, ta, tb, a, b, c, alpha=1.0, beta=0.0, flags=0):
+        m, n = c.shape
+        k = a.shape[1] if ta == "N" else a.shape[0]
+        A = np.asfortranarray(a, dtype=np.float64); B = np.asfortranarray(b, dtype=np.float64)
+        Cm = np.asfortranarray(c, dtype=np.float64).copy(order="F")
+        self.check(self.lib.dftbgpu_test_dgemm(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
+                                               _p(A, C.c_double), _p(B, C.c_double), beta, _p(Cm, C.c_double), flags))
+        return Cm
+
+    def test_tridiag(self, a):
+        n = a.shape[0]
+        A = np.asfortranarray(a, dtype=np.float64)
+        d = np.zeros(n); e = np.zeros(max(n - 1, 1))
+        self.check(self.lib.dftbgpu_test_tridiag(self.h, n, _p(A, C.c_double), _p(d, C.c_double), _p(e, C.c_double)))
+        return d, e[:n - 1]
+
+    def test_stedc(self, d, e):
+        n = len(d)
+        dd = np.array(d, dtype=np.float64); ee = np.zeros(max(n - 1, 1)); ee[:n - 1] = e
+        q = np.zeros((n, n), order="F")
+        self.check(self.lib.dftbgpu_test_stedc(self.h, n, _p(dd, C.c_double), _p(ee, C.c_double), _p(q, C.c_double)))
+        return dd, q
+
     def kernel_launches(self) -> int:
         return int(self.lib.dftbgpu_kernel_launches(self.h))
+
+    def profile(self, enable: bool):
+        self.check(self.lib.dftbgpu_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        n = len(PHASES)
+        ms = np.zeros(n); fl = np.zeros(n); calls = np.zeros(n, dtype=np.int64)
+        self.lib.dftbgpu_profile_read(self.h, n, _p(ms, C.c_double), _p(fl, C.c_double),
+                                      calls.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return {name: dict(ms=float(ms[i]), flops=float(fl[i]), calls=int(calls[i])) for i, name in enumerate(PHASES)}
+
+    def set_geometry_dev(self, coords_dev_ptr: int, species: np.ndarray):
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        self.check(self.lib.dftbgpu_set_geometry_dev(self.h, len(sp), C.c_void_p(coords_dev_ptr), _p(sp, C.c_int)))
+        self.natom = len(sp)
+        n = C.c_int()
+        self.check(self.lib.dftbgpu_n_orbitals(self.h, C.byref(n)))
+        self.norb = n.value
+
+    def scc_lite(self, opts: SccOpts) -> dict:
+        """SCC returning only energies and iteration count (no host copies of vectors)."""
+        en = Energies()
+        nit = C.c_int()
+        conv = C.c_int()
+        self.check(self.lib.dftbgpu_scc(self.h, C.byref(opts), None, C.byref(en), None, None, None, None,
+                                        C.byref(nit), C.byref(conv)))
+        return dict(energies=en.as_dict(), n_iter=nit.value, converged=bool(conv.value))
+
+    def gradients_dev(self, grad_dev_ptr: int):
+        self.check(self.lib.dftbgpu_gradients_dev(self.h, C.c_void_p(grad_dev_ptr)))
 
 
 def default_opts(**kw) -> SccOpts:

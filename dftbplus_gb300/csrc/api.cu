@@ -60,7 +60,59 @@ struct Ctx {
   int nlevels = 0;
   bool have_w = false;
   double nel = 0.0;
+  // phase timers (CUDA events on the stream)
+  bool prof = false;
+  std::vector<std::pair<int, cudaEvent_t>> marks;
+  double prof_ms[kNPhase] = {0};
+  double prof_flops[kNPhase] = {0};
+  long long prof_calls[kNPhase] = {0};
 };
+
+// Record the start of a phase (phase < 0 closes the previous one).
+static void mark(Ctx *c, int phase) {
+  if (!c->prof) return;
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, c->stream);
+  c->marks.push_back({phase, e});
+}
+
+static void prof_flops(Ctx *c, int phase, double f) {
+  if (c->prof) c->prof_flops[phase] += f;
+}
+
+// Accumulate elapsed times between consecutive marks (called where the host synchronises anyway).
+static void flush_marks(Ctx *c) {
+  if (!c->prof || c->marks.empty()) return;
+  cudaEventSynchronize(c->marks.back().second);
+  for (size_t i = 0; i + 1 < c->marks.size(); ++i) {
+    int ph = c->marks[i].first;
+    if (ph < 0) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->marks[i].second, c->marks[i + 1].second);
+    c->prof_ms[ph] += ms;
+    c->prof_calls[ph] += 1;
+  }
+  for (size_t i = 0; i + 1 < c->marks.size(); ++i) cudaEventDestroy(c->marks[i].second);
+  std::pair<int, cudaEvent_t> last = c->marks.back();
+  c->marks.clear();
+  if (last.first >= 0) c->marks.push_back(last);
+  else cudaEventDestroy(last.second);
+  // GEMM launches
+  auto &gp = g_gemm_prof;
+  for (size_t i = 0; i + 1 < gp.ev.size(); i += 2) {
+    cudaEventSynchronize(gp.ev[i + 1]);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, gp.ev[i], gp.ev[i + 1]);
+    c->prof_ms[kPhGemm] += ms;
+    c->prof_flops[kPhGemm] += gp.flops[i / 2];
+    c->prof_calls[kPhGemm] += 1;
+    cudaEventDestroy(gp.ev[i]);
+    cudaEventDestroy(gp.ev[i + 1]);
+  }
+  gp.ev.clear();
+  gp.flops.clear();
+}
 
 int set_error(Ctx *c, int code, const char *fmt, ...) {
   if (c) {
@@ -219,16 +271,25 @@ static int check_status(Ctx *c, const char *stage) {
 template <class PickK>
 static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k) {
   cudaStream_t s = c->stream;
+  const double nd = (double)n;
   // A = L^-1 H L^-T : T = H L^-T (L^-T upper), A(lower) = L^-1 T (L^-1 lower)
+  mark(c, kPhTransform);
+  prof_flops(c, kPhTransform, nd * nd * nd);
   dgemm(s, 'N', 'T', n, n, n, 1.0, Hm, n, c->Linv, n, 0.0, c->T, n, kBUpper);
   dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, Hm, n, kALower | kCLower);
+  mark(c, kPhSytrd);
+  prof_flops(c, kPhSytrd, 4.0 / 3.0 * nd * nd * nd);
   sytrd_lower(s, n, Hm, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
+  mark(c, kPhStedc);
   int rc = stedc(s, n, c->dd, c->ee, c->Z, n, c->wk_stedc, c->iwk_stedc, c->d_status);
   if (rc != 0) return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
   DG_CUDA(c, cudaMemcpyAsync(c->eig, c->dd, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  mark(c, kPhFermi);
   int k = 0;
   DG_CHECK(c, pick_k(&k));
+  mark(c, kPhBack);
   if (k > 0) {
+    prof_flops(c, kPhBack, 3.0 * nd * nd * (double)k);
     ormtr_left(s, n, k, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
     dgemm(s, 'T', 'N', n, k, n, 1.0, c->Linv, n, c->Z, n, 0.0, c->C, n, kAUpper);
   }
@@ -462,6 +523,8 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
     }
   }
   c->npairs = np;
+  mark(c, kPhH0S);
+  prof_flops(c, kPhH0S, (double)norb * norb * norb / 3.0);
   build_h0_s(s, m, g, c->d_pi, c->d_pj, np, c->H0, c->S);
   repulsive_energy(s, m, g, c->d_eatom, c->d_scal);
   // Cholesky of S (in Z as scratch) and L^-1
@@ -469,8 +532,10 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   potrf_lower(s, norb, c->Z, norb, c->d_status);
   DG_CHECK(c, check_status(c, "Cholesky of S"));
   trtri_lower(s, norb, c->Z, norb, c->Linv, norb, c->T);
+  mark(c, -1);
   DG_CUDA(c, cudaGetLastError());
   DG_CUDA(c, cudaStreamSynchronize(s));
+  flush_marks(c);
   c->have_geom = true;
   c->have_scc = false;
   c->have_w = false;
@@ -509,6 +574,7 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   int it = 0;
   bool conv = false;
   for (it = 1; it <= o->max_iter; ++it) {
+    mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
     assemble_h(s, g, c->H0, c->S, c->d_V, c->H);
     int k = 0;
@@ -526,15 +592,21 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     DG_CHECK(c, eigensolve(c, n, c->H, pick));
     k = (int)h_scal[kSNLevels];
     c->nlevels = k;
+    mark(c, kPhDensity);
+    prof_flops(c, kPhDensity, (double)n * n * k);
     DG_CHECK(c, density(c, n, k, c->fill, c->rho));
+    mark(c, kPhMulliken);
     mulliken(s, g, c->rho, c->S, c->H0, c->qorb, c->d_qout, c->eorb, c->d_scal);
     potential(s, m, g, c->d_qout, c->d_q0, c->d_Vout);
     scc_energy(s, N, c->d_Vout, c->d_qout, c->d_q0, c->d_scal);
+    mark(c, kPhBroyden);
     broyden_step(s, N, it, o->min_iter, o->max_iter, o->scc_tol, o->mix_alpha, o->mix_omega0, o->mix_min_weight,
                  o->mix_max_weight, o->mix_weight_fac, c->bro, c->d_qin, c->d_qout, c->d_scal);
+    mark(c, -1);
     DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
     DG_CUDA(c, cudaGetLastError());
+    flush_marks(c);
     conv = h_scal[kSConv] != 0.0;
     if (conv) break;
   }
@@ -568,6 +640,8 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
   cudaSetDevice(c->device);
   cudaStream_t s = c->stream;
   const int n = c->norb;
+  mark(c, kPhForces);
+  prof_flops(c, kPhForces, (double)n * n * c->nlevels);
   energy_weights(s, c->nlevels, c->fill, c->eig, c->fe);
   DG_CHECK(c, density(c, n, c->nlevels, c->fe, c->W));
   c->have_w = true;
@@ -575,6 +649,7 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
   ModelDev m = model_view(c);
   gradient_bands(s, m, g, c->rho, c->W, c->d_Vout, c->d_grad);
   gradient_dc_rep(s, m, g, c->d_qout, c->d_q0, c->d_grad);
+  mark(c, -1);
   DG_CUDA(c, cudaGetLastError());
   if (dev) {
     DG_CUDA(c, cudaMemcpyAsync(grad, c->d_grad, sizeof(double) * 3 * c->natom, cudaMemcpyDeviceToDevice, s));
@@ -583,7 +658,38 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
     DG_CUDA(c, cudaMemcpyAsync(grad, c->d_grad, sizeof(double) * 3 * c->natom, cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
   }
+  flush_marks(c);
   return DFTBGPU_OK;
+}
+
+int dftbgpu_profile_enable(dftbgpu_ctx *c, int enable) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  flush_marks(c);
+  for (auto &mk : c->marks) cudaEventDestroy(mk.second);
+  c->marks.clear();
+  if (enable) {
+    for (int i = 0; i < kNPhase; ++i) {
+      c->prof_ms[i] = 0.0;
+      c->prof_flops[i] = 0.0;
+      c->prof_calls[i] = 0;
+    }
+  }
+  c->prof = enable != 0;
+  g_gemm_prof.on = enable != 0;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_profile_read(dftbgpu_ctx *c, int nphase, double *ms, double *flops, long long *calls) {
+  if (!c || nphase < 0) return DFTBGPU_ERR_ARGS;
+  int k = std::min(nphase, (int)kNPhase);
+  for (int i = 0; i < k; ++i) {
+    if (ms) ms[i] = c->prof_ms[i];
+    if (flops) flops[i] = c->prof_flops[i];
+    if (calls) calls[i] = c->prof_calls[i];
+  }
+  return k;
 }
 
 int dftbgpu_gradients(dftbgpu_ctx *c, double *grad) { return gradients_impl(c, grad, false); }
@@ -647,6 +753,67 @@ int dftbgpu_sygvd(dftbgpu_ctx *c, int n, double *a, double *b, double *w) {
   DG_CUDA(c, cudaMemcpyAsync(w, c->eig, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   DG_CUDA(c, cudaMemcpyAsync(a, c->C, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
   DG_CUDA(c, cudaStreamSynchronize(s));
+  return DFTBGPU_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int dftbgpu_test_dgemm(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *a,
+                       const double *b, double beta, double *cm, int flags) {
+  if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k < 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  int lda = TA ? std::max(k, 1) : m, ldb = TB ? n : std::max(k, 1);
+  size_t na = (size_t)lda * (TA ? m : std::max(k, 1)), nb = (size_t)ldb * (TB ? std::max(k, 1) : n);
+  double *dA, *dB, *dC;
+  DG_CUDA(c, cudaMalloc(&dA, na * 8));
+  DG_CUDA(c, cudaMalloc(&dB, nb * 8));
+  DG_CUDA(c, cudaMalloc(&dC, (size_t)m * n * 8));
+  DG_CUDA(c, cudaMemcpy(dA, a, na * 8, cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dB, b, nb * 8, cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dC, cm, (size_t)m * n * 8, cudaMemcpyHostToDevice));
+  dg::dgemm(s, ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, m, flags);
+  DG_CUDA(c, cudaStreamSynchronize(s));
+  DG_CUDA(c, cudaMemcpy(cm, dC, (size_t)m * n * 8, cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_test_tridiag(dftbgpu_ctx *c, int n, const double *a, double *d, double *e) {
+  if (!c || !a || !d || !e || n <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  DG_CHECK(c, ensure_orbitals(c, n));
+  DG_CUDA(c, cudaMemcpy(c->H, a, sizeof(double) * n * n, cudaMemcpyHostToDevice));
+  sytrd_lower(s, n, c->H, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
+  DG_CUDA(c, cudaStreamSynchronize(s));
+  DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
+  c->have_geom = false;
+  c->have_scc = false;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_test_stedc(dftbgpu_ctx *c, int n, double *d, const double *e, double *q) {
+  if (!c || !d || !q || n <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  DG_CHECK(c, ensure_orbitals(c, n));
+  DG_CUDA(c, cudaMemcpy(c->dd, d, sizeof(double) * n, cudaMemcpyHostToDevice));
+  if (n > 1) DG_CUDA(c, cudaMemcpy(c->ee, e, sizeof(double) * (n - 1), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemset(c->d_status, 0, sizeof(int)));
+  if (stedc(s, n, c->dd, c->ee, c->Z, n, c->wk_stedc, c->iwk_stedc, c->d_status) != 0)
+    return set_error(c, DFTBGPU_ERR_ARGS, "stedc layout");
+  DG_CHECK(c, check_status(c, "stedc"));
+  DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  DG_CUDA(c, cudaMemcpy(q, c->Z, sizeof(double) * n * n, cudaMemcpyDeviceToHost));
+  c->have_geom = false;
+  c->have_scc = false;
   return DFTBGPU_OK;
 }
 

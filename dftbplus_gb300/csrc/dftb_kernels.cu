@@ -115,6 +115,7 @@ __device__ double neville8(const double *col, double incr, double x, int il) {
 #pragma unroll
   for (int mm = 1; mm < 8; ++mm) delta[mm] = 1.0 / (xp[mm] - xp[0]);
   int icl = (int)ceil((x - xp[0]) * delta[1]);  // 1-based
+  icl = max(1, min(8, icl));                     // only binds for r < 4 grid steps (no valid pair)
   double y = col[il - 8 + icl - 1];
   icl -= 1;
 #pragma unroll

@@ -115,11 +115,34 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
   }
 }
 
+GemmProfile g_gemm_prof;
+
+static double gemm_executed_flops(int m, int n, int k, int flags) {
+  double f = 0.0;
+  for (int i0 = 0; i0 < m; i0 += 64)
+    for (int j0 = 0; j0 < n; j0 += 64) {
+      if ((flags & kCLower) && i0 + 63 < j0) continue;
+      int kmin = 0, kmax = k;
+      if (flags & kALower) kmax = std::min(kmax, i0 + 64);
+      if (flags & kAUpper) kmin = std::max(kmin, i0);
+      if (flags & kBLower) kmin = std::max(kmin, j0);
+      if (flags & kBUpper) kmax = std::min(kmax, j0 + 64);
+      if (kmax > kmin) f += 2.0 * std::min(64, m - i0) * std::min(64, n - j0) * (double)(kmax - kmin);
+    }
+  return f;
+}
+
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags) {
   if (m <= 0 || n <= 0) return;
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64));
   bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (g_gemm_prof.on) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+  }
   if (!TA && !TB)
     dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
   else if (!TA && TB)
@@ -129,6 +152,12 @@ void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, 
   else
     dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
   count_launch();
+  if (g_gemm_prof.on) {
+    cudaEventRecord(e1, s);
+    g_gemm_prof.ev.push_back(e0);
+    g_gemm_prof.ev.push_back(e1);
+    g_gemm_prof.flops.push_back(gemm_executed_flops(m, n, k, flags));
+  }
 }
 
 // ------------------------------------------------------------------------------------- helpers

@@ -17,6 +17,15 @@ enum GemmFlags : int {
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0);
 
+// Optional timing of every dgemm launch (events around each launch, executed FLOPs counted from
+// the tile k-ranges the kernel actually iterates). Enabled by the context's profiler.
+struct GemmProfile {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;     // pairs (start, stop)
+  std::vector<double> flops;       // per pair
+};
+extern GemmProfile g_gemm_prof;
+
 // In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
 void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);
 

@@ -44,14 +44,16 @@ __device__ __forceinline__ double wmax(double v) {
   return v;
 }
 
-// Tear: d[m-1] -= |e[m-1]|, d[m] -= |e[m-1]| for every block boundary m; leaves Q = I.
-__global__ void dc_tear_kernel(int n, double *d, const double *e, const int *bounds, int nb) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nb) return;
-  int m = bounds[k];
-  double b = fabs(e[m - 1]);
-  d[m - 1] -= b;
-  d[m] -= b;
+// Tear: d[m-1] -= |e[m-1]|, d[m] -= |e[m-1]| for every block boundary m. Leaves are single
+// elements, so every m in 1..n-1 is a boundary and each diagonal entry loses both neighbours'
+// couplings (one thread per entry: adjacent boundaries share an entry).
+__global__ void dc_tear_kernel(int n, double *d, const double *e) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = d[i];
+  if (i > 0) v -= fabs(e[i - 1]);
+  if (i < n - 1) v -= fabs(e[i]);
+  d[i] = v;
 }
 
 __global__ void dc_identity_kernel(int n, double *Q, int ldq) {
@@ -237,18 +239,21 @@ __global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_mer
   const double dorg = dl[org];
   bool conv = false;
   for (int it = 0; it < kSecularMaxIter; ++it) {
-    double sf = 0.0, sp = 0.0, sq = 0.0;
+    double sf = 0.0, sp = 0.0, sq = 0.0, sa = 0.0;
     for (int j = lane; j < K; j += 32) {
       double dd = (dl[j] - dorg) - tau;
       double t = w[j] * w[j] / dd;
       sf += t;
+      sa += fabs(t);
       if (j <= i) sp += t / dd; else sq += t / dd;
     }
     double f = 1.0 + rho * wsum(sf);
     double psip = rho * wsum(sp);
     double phip = rho * wsum(sq);
+    // rounding-error bound of the evaluated f (cf. the ERRETM test of LAPACK's dlaed4)
+    double ferr = kEps * (8.0 * (1.0 + rho * wsum(sa)) + fabs(tau) * (psip + phip));
     if (f > 0.0) hi = tau; else lo = tau;
-    if (f == 0.0) { conv = true; break; }
+    if (fabs(f) <= ferr) { conv = true; break; }
     double nt;
     if (i < K - 1) {
       double dlo = (dl[i] - dorg) - tau, dhi = (dl[i + 1] - dorg) - tau;
@@ -527,8 +532,11 @@ int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, doubl
   // the metadata lives in a dedicated device allocation owned by the caller's iwork tail
   cudaMemcpyAsync(dev_meta, meta.data(), meta.size() * sizeof(int), cudaMemcpyHostToDevice, s);
 
-  dc_tear_kernel<<<ceil_div((int)bounds.size(), 256), 256, 0, s>>>(n, d, e, dev_meta, (int)bounds.size());
+  dc_tear_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
   count_launch();
+  // The merge at level L reads whole blocks [a,b)^2 whose off-diagonal sub-blocks must be zero;
+  // the scatter only writes inside the current blocks, so the second buffer starts zeroed.
+  cudaMemsetAsync(W.Qalt, 0, sizeof(double) * (size_t)n * n, s);
 
   double *Qin = Q, *Qout = W.Qalt;
   std::vector<int> hK;

@@ -137,6 +137,31 @@ int dftbgpu_get_matrix(dftbgpu_ctx *ctx, int which, double *out);
 /* Number of this library's kernel launches since creation (for launch accounting). */
 long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
 
+/*
+ * Phase timers measured with CUDA events on the context's stream (the GPU counterpart of the
+ * reference's timer tree, common/environment.F90:97-133). Phases, in order:
+ *   0 H0/S build + Cholesky, 1 potentials + H assembly, 2 L^-1 H L^-T, 3 tridiagonalisation,
+ *   4 tridiagonal divide and conquer, 5 Fermi filling, 6 back-transformation (Q Z, L^-T Y),
+ *   7 density matrix, 8 Mulliken + energies, 9 Broyden mixing, 10 gradients, 11 FP64 GEMM (all
+ *   GEMM launches, overlapping the phases above).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[12], flops[12] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[12]; returns the number of phases written.
+ */
+int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
+int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);
+
+/*
+ * Stage-level test hooks (host arrays; used by the parity tests to check each eigensolver stage on
+ * its own; they have no counterpart in the reference).
+ *   dgemm:   c = alpha op(a) op(b) + beta c (column-major, lda=m or k as for op 'N'/'T').
+ *   tridiag: Householder reduction of the symmetric a (n x n) -> d[n], e[n-1].
+ *   stedc:   eigenpairs of the tridiagonal (d, e): d <- eigenvalues ascending, q[n*n] vectors.
+ */
+int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
+                       const double *a, const double *b, double beta, double *c, int flags);
+int dftbgpu_test_tridiag(dftbgpu_ctx *ctx, int n, const double *a, double *d, double *e);
+int dftbgpu_test_stedc(dftbgpu_ctx *ctx, int n, double *d, const double *e, double *q);
+
 #ifdef __cplusplus
 }
 #endif
