@@ -67,6 +67,7 @@ SIGNATURES = {
     "dftbgpu_test_stedc": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "dftbgpu_profile_read": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.POINTER(C.c_longlong)]),
+    "dftbgpu_stedc_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",

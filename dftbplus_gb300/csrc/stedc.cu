@@ -583,4 +583,148 @@ int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, doubl
   return 0;
 }
 
+// ------------------------------------------------------------------------------------- no-alloc
+// Allocation-free variant for callers that cannot allocate device memory (a solver step running
+// inside CUDA stream capture, where cudaMalloc is not permitted; a host program whose device memory
+// is owned by another allocator or pool; an MD loop that must not trigger the device-wide
+// synchronisation cudaMalloc implies). All scratch lives in one file-scope device array sized for
+// n <= kNoAllocMaxN, and the level plan is built on the device, so no host or device memory is
+// allocated per call.
+constexpr int kNoAllocMaxN = 256;
+constexpr int kNoAllocMaxLevels = 8;                   // ceil(log2 256)
+constexpr size_t kNoAllocWork = 9 * 256 + 2 * 256 + 4 * 256 * 256 + 64;      // doubles
+constexpr size_t kNoAllocPlan = 4 * 256 + 2 * 256 * kNoAllocMaxLevels + 64;  // ints
+constexpr size_t kNoAllocIwork = 10 * 256 + kNoAllocPlan + 64;                // ints
+constexpr size_t kNoAllocDoubles = kNoAllocWork + (kNoAllocIwork + 1) / 2 + 32;
+
+// ~2.2 MB per device, held by every GPU that loads the library until process exit. Shared by all
+// calls: it keeps the previous call's contents, and calls that overlap on the GPU race on it.
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+struct DcPlanOffsets {
+  int nlev;
+  int nm[kNoAllocMaxLevels + 1];
+  int off_merge[kNoAllocMaxLevels + 1], off_pm[kNoAllocMaxLevels + 1], off_pma[kNoAllocMaxLevels + 1];
+};
+
+// The pairwise merge tree of single-element leaves has blocks of 2^L elements at level L
+// (the last one truncated; a block without a right half passes through unchanged).
+__global__ void dc_plan_kernel(int n, DcPlanOffsets P, int *meta) {
+  for (int L = 1; L <= P.nlev; ++L) {
+    const int size = 1 << L;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+      int mi = g >> L;
+      int a = mi << L;
+      int b = min(a + size, n);
+      int m = min(a + (size >> 1), b);
+      meta[P.off_pma[L] + g] = mi;
+      meta[P.off_pm[L] + g] = (m == b) ? -1 : mi;
+      if (g == a) {
+        int *mg = meta + P.off_merge[L] + 4 * mi;
+        mg[0] = a; mg[1] = m; mg[2] = b; mg[3] = 0;
+      }
+    }
+  }
+}
+
+static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_in, double *Q, double *scratch) {
+  double *e = const_cast<double *>(e_in);  // read only
+  DcWork W;
+  double *p = scratch;
+  W.Ds = p; p += n; W.zs = p; p += n; W.dl = p; p += n; W.w = p; p += n; W.tau = p; p += n;
+  W.lam = p; p += n; W.zh = p; p += n; W.vals = p; p += n; p += n;
+  W.rot_cs = p; p += 2 * (size_t)n;
+  W.Gs = p; p += (size_t)n * n; W.U = p; p += (size_t)n * n; W.Qtmp = p; p += (size_t)n * n;
+  W.Qalt = p;
+  int *ip = reinterpret_cast<int *>(scratch + kNoAllocWork);
+  int *status = ip; ip += 32;
+  W.perm = ip; ip += n; W.ndpos = ip; ip += n; W.dfpos = ip; ip += n; W.org = ip; ip += n;
+  W.srcinfo = ip; ip += n; W.mK = ip; ip += n; W.mRot = ip; ip += n; ip += n;
+  W.rot_cols = ip; ip += 2 * (size_t)n;
+  int *meta = ip;
+
+  DcPlanOffsets P{};
+  int nlev = 0;
+  while ((1 << nlev) < n) ++nlev;
+  P.nlev = nlev;
+  int off = 0;
+  for (int L = 1; L <= nlev; ++L) {
+    P.nm[L] = (n + (1 << L) - 1) >> L;
+    P.off_merge[L] = off; off += 4 * P.nm[L];
+    P.off_pm[L] = off; off += n;
+    P.off_pma[L] = off; off += n;
+  }
+  cudaMemsetAsync(status, 0, sizeof(int), s);
+  dim3 gi(ceil_div(n, 256), n);
+  dc_identity_kernel<<<gi, 256, 0, s>>>(n, Q, n);
+  count_launch();
+  if (n == 1) return 0;
+  dc_plan_kernel<<<1, 256, 0, s>>>(n, P, meta);
+  dc_tear_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
+  count_launch(2);
+  cudaMemsetAsync(W.Qalt, 0, sizeof(double) * (size_t)n * n, s);
+  double *Qin = Q, *Qout = W.Qalt;
+  for (int L = 1; L <= nlev; ++L) {
+    const Merge *dm = reinterpret_cast<const Merge *>(meta + P.off_merge[L]);
+    const int *pm = meta + P.off_pm[L];
+    const int *pma = meta + P.off_pma[L];
+    const int nm = P.nm[L];
+    const int max_block = std::min(1 << L, n);
+    dc_sort_kernel<<<nm, 256, 0, s>>>(dm, d, e, Qin, n, W);
+    dc_deflate_kernel<<<nm, 256, 0, s>>>(dm, e, W);
+    dim3 gr(nm, ceil_div(max_block, 256));
+    dc_rotate_kernel<<<gr, 256, 0, s>>>(dm, Qin, n, W);
+    int wb = ceil_div((long long)n * 32, 256);
+    dc_secular_kernel<<<wb, 256, 0, s>>>(n, dm, pm, e, W, status);
+    dc_zhat_kernel<<<wb, 256, 0, s>>>(n, dm, pm, e, W);
+    dc_build_u_kernel<<<wb, 256, 0, s>>>(n, dm, pm, W, n);
+    dc_gather_kernel<<<n, 128, 0, s>>>(n, dm, pm, Qin, n, W, n);
+    count_launch(7);
+    if (max_block <= kSmallMerge) {
+      dc_small_gemm_kernel<<<nm, 256, 0, s>>>(dm, W, n);
+      count_launch();
+    } else {
+      // at most two merges at this size (n <= 256): read their sizes into a stack buffer
+      int hK[2] = {0, 0};
+      cudaMemcpyAsync(hK, W.mK, sizeof(int) * std::min(nm, 2), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      for (int k = 0; k < std::min(nm, 2); ++k) {
+        int a = k << L, b = std::min(a + (1 << L), n), m = std::min(a + (1 << (L - 1)), b);
+        if (m == b || hK[k] == 0) continue;
+        dgemm(s, 'N', 'N', b - a, hK[k], hK[k], 1.0, W.Gs + a + (size_t)a * n, n, W.U + (size_t)a * n, n, 0.0,
+              W.Qtmp + a + (size_t)a * n, n);
+      }
+    }
+    dim3 grk(nm, ceil_div(max_block, 256));
+    dc_rank_kernel<<<grk, 256, 0, s>>>(dm, d, W);
+    dc_scatter_kernel<<<n, 128, 0, s>>>(n, pma, dm, Qin, n, Qout, d, W, n);
+    count_launch(2);
+    std::swap(Qin, Qout);
+  }
+  if (Qin != Q) cudaMemcpyAsync(Q, Qin, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
+  int st = 0;
+  cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
 }  // namespace dg
+
+// Per-device address of the scratch array, resolved once per device on the first call.
+static double *g_noalloc_dev_ptr[64] = {nullptr};
+
+extern "C" int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *stream) {
+  if (n < 1 || n > dg::kNoAllocMaxN || !d || !q || (n > 1 && !e)) return DFTBGPU_ERR_ARGS;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DFTBGPU_ERR_CUDA;
+  if (!g_noalloc_dev_ptr[dev]) {
+    double *ptr = nullptr;
+    if (cudaGetSymbolAddress((void **)&ptr, dg::g_noalloc_scratch) != cudaSuccess || !ptr) return DFTBGPU_ERR_CUDA;
+    g_noalloc_dev_ptr[dev] = ptr;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = dg::stedc_noalloc_impl(s, n, d, e, q, g_noalloc_dev_ptr[dev]);
+  if (cudaGetLastError() != cudaSuccess) return DFTBGPU_ERR_CUDA;
+  if (st == dg::kDevIterCap) return DFTBGPU_ERR_ITER_CAP;
+  return st == 0 ? DFTBGPU_OK : DFTBGPU_ERR_CUDA;
+}

@@ -151,6 +151,23 @@ int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);
 
 /*
+ * Allocation-free tridiagonal divide and conquer. This entry point has no counterpart in the
+ * reference. It serves callers that cannot allocate device memory: a solver step recorded into a
+ * CUDA graph (cudaMalloc is not permitted during stream capture), a host program whose device
+ * memory belongs to another allocator or pool, or a dynamics loop that must avoid the device-wide
+ * synchronisation an allocation implies. It needs no context.
+ *   n in 1..256 (larger n returns DFTBGPU_ERR_ARGS and does nothing);
+ *   d[n] (device): diagonal in, eigenvalues ascending out; e[n-1] (device): off-diagonal, read only;
+ *   q[n*n] (device, column-major): eigenvectors out; stream: cudaStream_t or NULL (legacy default).
+ * The caller passes inputs and outputs; all scratch is one file-scope device array of about 2.2 MB
+ * that every GPU loading the library keeps until process exit. The first call on a device looks
+ * up that array's device address (make it before any stream capture). Calls share the array, so
+ * calls that overlap on the GPU (other streams or threads) race and must be serialised by the
+ * caller. Returns 0, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_ITER_CAP or DFTBGPU_ERR_CUDA.
+ */
+int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *stream);
+
+/*
  * Stage-level test hooks (host arrays; used by the parity tests to check each eigensolver stage on
  * its own; they have no counterpart in the reference).
  *   dgemm:   c = alpha op(a) op(b) + beta c (column-major, lda=m or k as for op 'N'/'T').
