@@ -45,6 +45,8 @@ struct Ctx {
   size_t cap_n = 0;
   double *H0 = nullptr, *S = nullptr, *Linv = nullptr, *H = nullptr, *T = nullptr, *Vh = nullptr,
          *Z = nullptr, *C = nullptr, *rho = nullptr, *W = nullptr;
+  double *Lc = nullptr;   // Cholesky factor of S (lower)
+  double *A0 = nullptr;   // L^-1 H0 L^-T (lower), per geometry
   double *eig = nullptr, *fill = nullptr, *fe = nullptr, *dd = nullptr, *ee = nullptr, *tau = nullptr,
          *qorb = nullptr, *eorb = nullptr;
   double *wk_sytrd = nullptr, *wk_ormtr = nullptr, *wk_stedc = nullptr;
@@ -224,7 +226,8 @@ static int ensure_atoms(Ctx *c, int natom) {
 static int ensure_orbitals(Ctx *c, int n) {
   if ((size_t)n <= c->cap_n) return DFTBGPU_OK;
   size_t nn = (size_t)n * n;
-  for (double **p : {&c->H0, &c->S, &c->Linv, &c->H, &c->T, &c->Vh, &c->Z, &c->C, &c->rho, &c->W})
+  for (double **p : {&c->H0, &c->S, &c->Linv, &c->H, &c->T, &c->Vh, &c->Z, &c->C, &c->rho, &c->W, &c->Lc,
+                     &c->A0})
     DG_CHECK(c, dev_alloc(c, p, nn));
   for (double **p : {&c->eig, &c->fill, &c->fe, &c->dd, &c->ee, &c->tau, &c->qorb, &c->eorb})
     DG_CHECK(c, dev_alloc(c, p, (size_t)n));
@@ -269,14 +272,16 @@ static int check_status(Ctx *c, const char *stage) {
 // c->eig; the eigenvectors of the first k levels into c->C (columns), k chosen by pick_k after the
 // eigenvalues are known (the Fermi filling decides how many levels the density matrix needs).
 template <class PickK>
-static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k) {
+static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = false) {
   cudaStream_t s = c->stream;
   const double nd = (double)n;
-  // A = L^-1 H L^-T : T = H L^-T (L^-T upper), A(lower) = L^-1 T (L^-1 lower)
-  mark(c, kPhTransform);
-  prof_flops(c, kPhTransform, nd * nd * nd);
-  dgemm(s, 'N', 'T', n, n, n, 1.0, Hm, n, c->Linv, n, 0.0, c->T, n, kBUpper);
-  dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, Hm, n, kALower | kCLower);
+  if (!reduced) {
+    // A = L^-1 H L^-T : T = H L^-T (L^-T upper), A(lower) = L^-1 T (L^-1 lower)
+    mark(c, kPhTransform);
+    prof_flops(c, kPhTransform, nd * nd * nd);
+    dgemm(s, 'N', 'T', n, n, n, 1.0, Hm, n, c->Linv, n, 0.0, c->T, n, kBUpper);
+    dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, Hm, n, kALower | kCLower);
+  }
   mark(c, kPhSytrd);
   prof_flops(c, kPhSytrd, 4.0 / 3.0 * nd * nd * nd);
   sytrd_lower(s, n, Hm, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
@@ -360,7 +365,7 @@ int dftbgpu_destroy(dftbgpu_ctx *c) {
   void *ptrs[] = {c->d_sp, c->d_pair, c->d_tab, c->d_rep, c->d_xyz, c->d_species, c->d_orb, c->d_pcount,
                   c->d_pstart, c->d_pi, c->d_pj, c->d_q0, c->d_qin, c->d_qout, c->d_V, c->d_Vout,
                   c->d_eatom, c->d_grad, c->H0, c->S, c->Linv, c->H, c->T, c->Vh, c->Z, c->C, c->rho,
-                  c->W, c->eig, c->fill, c->fe, c->dd, c->ee, c->tau, c->qorb, c->eorb, c->wk_sytrd,
+                  c->W, c->Lc, c->A0, c->eig, c->fill, c->fe, c->dd, c->ee, c->tau, c->qorb, c->eorb, c->wk_sytrd,
                   c->wk_ormtr, c->wk_stedc, c->iwk_stedc, c->d_status, c->d_scal, c->bro.ww, c->bro.aa,
                   c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast};
   for (void *p : ptrs)
@@ -527,11 +532,13 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   prof_flops(c, kPhH0S, (double)norb * norb * norb / 3.0);
   build_h0_s(s, m, g, c->d_pi, c->d_pj, np, c->H0, c->S);
   repulsive_energy(s, m, g, c->d_eatom, c->d_scal);
-  // Cholesky of S (in Z as scratch) and L^-1
-  DG_CUDA(c, cudaMemcpyAsync(c->Z, c->S, sizeof(double) * (size_t)norb * norb, cudaMemcpyDeviceToDevice, s));
-  potrf_lower(s, norb, c->Z, norb, c->d_status);
+  // Cholesky of S, L^-1, and the reduced non-SCC Hamiltonian A0 = L^-1 H0 L^-T (lower)
+  DG_CUDA(c, cudaMemcpyAsync(c->Lc, c->S, sizeof(double) * (size_t)norb * norb, cudaMemcpyDeviceToDevice, s));
+  potrf_lower(s, norb, c->Lc, norb, c->d_status);
   DG_CHECK(c, check_status(c, "Cholesky of S"));
-  trtri_lower(s, norb, c->Z, norb, c->Linv, norb, c->T);
+  trtri_lower(s, norb, c->Lc, norb, c->Linv, norb, c->T, (size_t)norb * norb);
+  dgemm(s, 'N', 'T', norb, norb, norb, 1.0, c->H0, norb, c->Linv, norb, 0.0, c->T, norb, kBUpper);
+  dgemm(s, 'N', 'N', norb, norb, norb, 1.0, c->Linv, norb, c->T, norb, 0.0, c->A0, norb, kALower | kCLower);
   mark(c, -1);
   DG_CUDA(c, cudaGetLastError());
   DG_CUDA(c, cudaStreamSynchronize(s));
@@ -576,7 +583,12 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   for (it = 1; it <= o->max_iter; ++it) {
     mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
-    assemble_h(s, g, c->H0, c->S, c->d_V, c->H);
+    // reduced problem A = L^-1 H L^-T = A0 + 1/2 (B + B^T), B = L^-1 (diag(V) L)
+    mark(c, kPhTransform);
+    prof_flops(c, kPhTransform, (double)n * n * n);
+    reduced_shift(s, g, c->Lc, c->d_V, c->T);
+    dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
+    add_half_lower(s, n, c->A0, c->C, c->H);
     int k = 0;
     auto pick = [&](int *kout) -> int {
       fermi_filling(s, n, c->eig, nel, o->kT, c->fill, c->d_scal);
@@ -589,7 +601,7 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       *kout = (int)h_scal[kSNLevels];
       return DFTBGPU_OK;
     };
-    DG_CHECK(c, eigensolve(c, n, c->H, pick));
+    DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true));
     k = (int)h_scal[kSNLevels];
     c->nlevels = k;
     mark(c, kPhDensity);
@@ -740,7 +752,7 @@ int dftbgpu_sygvd(dftbgpu_ctx *c, int n, double *a, double *b, double *w) {
   DG_CHECK(c, check_status(c, "sygvd Cholesky"));
   // the caller's b receives L; keep a copy because Z is reused by the tridiagonal solver
   DG_CUDA(c, cudaMemcpyAsync(b, c->Z, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
-  trtri_lower(s, n, c->Z, n, c->Linv, n, c->T);
+  trtri_lower(s, n, c->Z, n, c->Linv, n, c->T, (size_t)n * n);
   // the SCC state (if any) no longer matches the stored L^-1
   c->have_geom = false;
   c->have_scc = false;

@@ -423,6 +423,39 @@ __global__ void orb_atom_kernel(GeomDev g, int *orb_atom) {
   for (int o = g.orb_off[a]; o < g.orb_off[a + 1]; ++o) orb_atom[o] = a;
 }
 
+// DL = diag(V_orb) L on the lower triangle (zero above): the SCC shift enters the reduced problem
+// only through B = L^-1 (D L), since L^-1 (H0 + 1/2 (D S + S D)) L^-T = A0 + 1/2 (B + B^T).
+__global__ void scale_rows_lower_kernel(int n, const int *orb_atom, const double *L, const double *V,
+                                        double *DL) {
+  int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    size_t idx = i + (size_t)j * n;
+    DL[idx] = (i >= j) ? V[orb_atom[i]] * L[idx] : 0.0;
+  }
+}
+
+// A (lower) = A0 + 1/2 (B + B^T) for lower-triangular B: off-diagonal A0 + B/2, diagonal A0 + B.
+__global__ void add_half_lower_kernel(int n, const double *A0, const double *B, double *A) {
+  int j = blockIdx.y;
+  for (int i = j + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    size_t idx = i + (size_t)j * n;
+    A[idx] = A0[idx] + ((i == j) ? B[idx] : 0.5 * B[idx]);
+  }
+}
+
+void reduced_shift(cudaStream_t s, const GeomDev &g, const double *L, const double *V, double *DL) {
+  const int *orb_atom = g.orb_off + g.natom + 1;
+  dim3 grid(std::min(ceil_div(g.norb, 256), 4), g.norb);
+  scale_rows_lower_kernel<<<grid, 256, 0, s>>>(g.norb, orb_atom, L, V, DL);
+  count_launch();
+}
+
+void add_half_lower(cudaStream_t s, int n, const double *A0, const double *B, double *A) {
+  dim3 grid(std::min(ceil_div(n, 256), 4), n);
+  add_half_lower_kernel<<<grid, 256, 0, s>>>(n, A0, B, A);
+  count_launch();
+}
+
 void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double *S, const double *V,
                 double *H) {
   // orb_off holds natom+1 entries followed by norb orbital->atom entries (see api.cu)

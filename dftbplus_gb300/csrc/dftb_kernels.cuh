@@ -41,6 +41,10 @@ void potential(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double
 // H = H0 + 1/2 S (V_mu + V_nu)
 void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double *S, const double *V,
                 double *H);
+// DL = diag(V_orb) L (lower), for B = L^-1 DL
+void reduced_shift(cudaStream_t s, const GeomDev &g, const double *L, const double *V, double *DL);
+// A(lower) = A0 + 1/2 (B + B^T), B lower triangular
+void add_half_lower(cudaStream_t s, int n, const double *A0, const double *B, double *A);
 // Fermi filling (spin unpolarised) from ascending eigenvalues; writes fill[n], scal[...]
 void fermi_filling(cudaStream_t s, int n, const double *eig, double nel, double kT, double *fill,
                    double *scal);

@@ -11,12 +11,15 @@ namespace dg {
 // ------------------------------------------------------------------------------------- GEMM
 // 64x64 output tile per CTA, 256 threads, 4x4 outputs per thread (strided by 16 so that shared
 // memory reads are conflict-free), K step 16, register prefetch of the next K slab.
+// With P != nullptr the CTA (x, y, z) sums only the z-th of gridDim.z slices of its k-range and
+// writes the raw sum to P + z*m*n (split-K; dgemm_splitk_reduce applies alpha/beta in a fixed
+// order, so results stay deterministic).
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double alpha,
                                                     const double *__restrict__ A, int lda,
                                                     const double *__restrict__ B, int ldb,
                                                     double beta, double *__restrict__ C, int ldc,
-                                                    int flags) {
+                                                    int flags, double *__restrict__ P) {
   constexpr int BM = 64, BN = 64, BK = 16;
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
@@ -29,6 +32,13 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
   if (flags & kAUpper) kmin = max(kmin, i0);
   if (flags & kBLower) kmin = max(kmin, j0);
   if (flags & kBUpper) kmax = min(kmax, j0 + BN);
+  if (P != nullptr && gridDim.z > 1) {
+    int span = max(kmax - kmin, 0);
+    int chunk = ((span + gridDim.z - 1) / gridDim.z + BK - 1) / BK * BK;
+    int lo = kmin + blockIdx.z * chunk;
+    kmax = min(kmax, lo + chunk);
+    kmin = lo;
+  }
 
   double acc[4][4];
 #pragma unroll
@@ -99,6 +109,20 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
       }
     }
   }
+  if (P != nullptr) {
+    double *Pz = P + (size_t)blockIdx.z * m * n;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int gi = i0 + tx + 16 * i;
+      if (gi >= m) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int gj = j0 + ty + 16 * j;
+        if (gj < n) Pz[gi + (size_t)gj * m] = acc[i][j];
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     int gi = i0 + tx + 16 * i;
@@ -112,6 +136,23 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
       if (beta != 0.0) v = fma(beta, *c, v);
       *c = v;
     }
+  }
+}
+
+// C = alpha * sum_z P[z] + beta * C over the tiles a split-K dgemm computed.
+__global__ void dgemm_splitk_reduce(int m, int n, int splits, const double *__restrict__ P, double alpha,
+                                    double beta, double *__restrict__ C, int ldc, int flags) {
+  size_t total = (size_t)m * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(idx % m), j = (int)(idx / m);
+    if ((flags & kCLower) && (i | 63) < (j & ~63)) continue;  // tile skipped by the GEMM
+    double s = 0.0;
+    for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + idx];
+    double *c = C + i + (size_t)j * ldc;
+    double v = alpha * s;
+    if (beta != 0.0) v = fma(beta, *c, v);
+    *c = v;
   }
 }
 
@@ -133,7 +174,8 @@ static double gemm_executed_flops(int m, int n, int k, int flags) {
 }
 
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
-           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags) {
+           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags, double *work,
+           size_t work_elems) {
   if (m <= 0 || n <= 0) return;
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64));
   bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
@@ -143,15 +185,33 @@ void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, 
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
   }
+  // Split-K when the output has too few tiles to fill the GPU and K is long.
+  int splits = 1;
+  long long tiles = (long long)grid.x * grid.y;
+  if (work && tiles < kSplitTarget && k >= 1024) {
+    long long sp = (kSplitTarget + tiles - 1) / tiles;
+    sp = std::min(sp, (long long)k / 256);
+    sp = std::min(sp, 64LL);
+    sp = std::min(sp, (long long)(work_elems / ((size_t)m * n)));
+    splits = (int)sp;
+    if (splits < 2) splits = 1;
+  }
+  double *P = (splits > 1) ? work : nullptr;
+  grid.z = splits;
   if (!TA && !TB)
-    dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+    dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else if (!TA && TB)
-    dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+    dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else if (TA && !TB)
-    dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+    dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else
-    dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+    dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   count_launch();
+  if (P) {
+    int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
+    dgemm_splitk_reduce<<<rb, 256, 0, s>>>(m, n, splits, P, alpha, beta, C, ldc, flags);
+    count_launch();
+  }
   if (g_gemm_prof.on) {
     cudaEventRecord(e1, s);
     g_gemm_prof.ev.push_back(e0);
@@ -328,16 +388,19 @@ __global__ void trtri_diag_kernel(int n, const double *L, int ldl, double *X, in
   }
 }
 
-void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work) {
+void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work,
+                 size_t work_elems) {
   // X must start zero outside the blocks that are written.
   set_zero(s, X, (size_t)ldx * n);
   int nblk = ceil_div(n, NB);
   trtri_diag_kernel<<<nblk, 256, 0, s>>>(n, L, ldl, X, ldx);
   count_launch();
+  double *sp = work + (size_t)NB * n;
+  size_t sp_elems = work_elems > (size_t)NB * n ? work_elems - (size_t)NB * n : 0;
   for (int b = 1; b < nblk; ++b) {
     int i0 = b * NB, jb = std::min(NB, n - i0);
     // T = L[i0:i0+jb, 0:i0] * X[0:i0, 0:i0]   (X lower)
-    dgemm(s, 'N', 'N', jb, i0, i0, 1.0, L + i0, ldl, X, ldx, 0.0, work, NB, kBLower);
+    dgemm(s, 'N', 'N', jb, i0, i0, 1.0, L + i0, ldl, X, ldx, 0.0, work, NB, kBLower, sp, sp_elems);
     // X[i0:, 0:i0] = -X_ii * T
     dgemm(s, 'N', 'N', jb, i0, jb, -1.0, X + i0 + (size_t)i0 * ldx, ldx, work, NB, 0.0, X + i0, ldx,
           kALower);
@@ -374,11 +437,11 @@ __device__ double block_sum(double v, double *sh) {
   return r;
 }
 
-// Step 1 of column j: apply the panel's previous reflectors to A(j:n, j), then generate the
-// reflector that annihilates A(j+2:n, j) (dlarfg semantics: beta = -sign(alpha) ||x||).
-__global__ void __launch_bounds__(RED_THREADS) latrd_column_kernel(
-    int n, int j, int jj, double *A, int lda, double *Vp, double *Wp, double *V, int ldv, double *d,
-    double *e, double *tau) {
+// Step 1a of column j (grid over rows): apply the panel's previous reflectors to A(j:n, j) and
+// write per-CTA partial sums of squares of A(j+2:n, j).
+__global__ void __launch_bounds__(256) latrd_update_kernel(int n, int j, int jj, double *A, int lda,
+                                                           const double *Vp, const double *Wp,
+                                                           double *part) {
   __shared__ double sh[32];
   __shared__ double coef[2 * PB];
   const int t = threadIdx.x;
@@ -389,43 +452,49 @@ __global__ void __launch_bounds__(RED_THREADS) latrd_column_kernel(
   __syncthreads();
   double *col = A + (size_t)j * lda;
   double sig = 0.0;
-  for (int r = j + t; r < n; r += RED_THREADS) {
+  for (int r = j + blockIdx.x * blockDim.x + t; r < n; r += gridDim.x * blockDim.x) {
     double a = col[r];
     for (int q = 0; q < jj; ++q)
       a -= Vp[r + (size_t)q * n] * coef[q] + Wp[r + (size_t)q * n] * coef[PB + q];
     col[r] = a;
     if (r >= j + 2) sig = fma(a, a, sig);
   }
-  sig = block_sum<RED_THREADS>(sig, sh);
-  // col[j], col[j+1] were written by threads 0 and 1 (r = j, j+1); make them visible.
-  __syncthreads();
-  __shared__ double s_scale, s_beta, s_tau;
-  if (t == 0) {
-    double dj = col[j];
-    d[j] = dj;
-    if (j + 1 < n) {
-      double alpha = col[j + 1];
-      double beta, tv, scale;
-      if (sig == 0.0) {
-        tv = 0.0;
-        beta = alpha;
-        scale = 0.0;
-      } else {
-        beta = -copysign(sqrt(alpha * alpha + sig), alpha);
-        tv = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-      }
+  sig = block_sum<256>(sig, sh);
+  if (t == 0) part[blockIdx.x] = sig;
+}
+
+// Step 1b (grid over rows): every CTA forms the same reflector from the partial sums (dlarfg
+// semantics: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta) and writes its rows of v.
+__global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, const double *A, int lda,
+                                                          const double *part, int nparts, double *Vp,
+                                                          double *V, int ldv, double *d, double *e,
+                                                          double *tau) {
+  __shared__ double s_scale;
+  const double *col = A + (size_t)j * lda;
+  if (threadIdx.x == 0) {
+    double sig = 0.0;
+    for (int i = 0; i < nparts; ++i) sig += part[i];
+    double alpha = col[j + 1];
+    double beta, tv, scale;
+    if (sig == 0.0) {
+      tv = 0.0;
+      beta = alpha;
+      scale = 0.0;
+    } else {
+      beta = -copysign(sqrt(alpha * alpha + sig), alpha);
+      tv = (beta - alpha) / beta;
+      scale = 1.0 / (alpha - beta);
+    }
+    s_scale = scale;
+    if (blockIdx.x == 0) {
+      d[j] = col[j];
       e[j] = beta;
       tau[j] = tv;
-      s_scale = scale;
-      s_beta = beta;
-      s_tau = tv;
     }
   }
   __syncthreads();
-  if (j + 1 >= n) return;
-  double scale = s_scale;
-  for (int r = t; r < n; r += RED_THREADS) {
+  const double scale = s_scale;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
     double v;
     if (r <= j) v = 0.0;
     else if (r == j + 1) v = 1.0;
@@ -587,7 +656,10 @@ void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e
     int nbp = std::min(PB, n - 1 - p0);
     for (int jj = 0; jj < nbp; ++jj) {
       int j = p0 + jj;
-      latrd_column_kernel<<<1, RED_THREADS, 0, s>>>(n, j, jj, A, lda, Vp, Wp, V, ldv, d, e, tau);
+      const int cb = std::min(ceil_div(n - j, 256), 64);
+      latrd_update_kernel<<<cb, 256, 0, s>>>(n, j, jj, A, lda, Vp, Wp, part);
+      latrd_house_kernel<<<cb, 256, 0, s>>>(n, j, jj, A, lda, part, cb, Vp, V, ldv, d, e, tau);
+      count_launch(2);
       int m = n - j - 1;
       int T = ceil_div(m, ST);
       const double *A22 = A + (j + 1) + (size_t)(j + 1) * lda;
@@ -640,7 +712,8 @@ __global__ void larft_kernel(int nb, const double *G, const double *tau, double 
 }
 
 size_t ormtr_work_size(int n, int k) {
-  return 2 * (size_t)OB * OB + 2 * (size_t)OB * std::max(k, 1);
+  // G, T, M, M2 + split-K partials (up to 8 slices of the larger of OB x k and OB x OB)
+  return 2 * (size_t)OB * OB + 2 * (size_t)OB * std::max(k, 1) + 8 * (size_t)OB * std::max(k, OB);
 }
 
 void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const double *tau, double *Z,
@@ -650,6 +723,8 @@ void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const do
   double *T = G + OB * OB;
   double *M = T + OB * OB;
   double *M2 = M + (size_t)OB * k;
+  double *SP = M2 + (size_t)OB * k;
+  const size_t sp_elems = 8 * (size_t)OB * std::max(k, OB);
   int nref = n - 1;  // reflectors j = 0 .. n-2
   int last = ((nref - 1) / OB) * OB;
   for (int p0 = last; p0 >= 0; p0 -= OB) {
@@ -657,10 +732,10 @@ void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const do
     int r0 = p0 + 1;          // first nonzero row of the block's vectors
     int mr = n - r0;
     const double *Vb = V + r0 + (size_t)p0 * ldv;
-    dgemm(s, 'T', 'N', nb, nb, mr, 1.0, Vb, ldv, Vb, ldv, 0.0, G, nb);
+    dgemm(s, 'T', 'N', nb, nb, mr, 1.0, Vb, ldv, Vb, ldv, 0.0, G, nb, 0, SP, sp_elems);
     larft_kernel<<<1, OB, 0, s>>>(nb, G, tau + p0, T);
     count_launch();
-    dgemm(s, 'T', 'N', nb, k, mr, 1.0, Vb, ldv, Z + r0, ldz, 0.0, M, nb);
+    dgemm(s, 'T', 'N', nb, k, mr, 1.0, Vb, ldv, Z + r0, ldz, 0.0, M, nb, 0, SP, sp_elems);
     dgemm(s, 'N', 'N', nb, k, nb, 1.0, T, nb, M, nb, 0.0, M2, nb, kAUpper);
     dgemm(s, 'N', 'N', mr, k, nb, -1.0, Vb, ldv, M2, nb, 1.0, Z + r0, ldz);
   }

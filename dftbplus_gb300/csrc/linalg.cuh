@@ -14,8 +14,12 @@ enum GemmFlags : int {
 };
 
 // C = alpha * op(A) * op(B) + beta * C ; op = 'N' or 'T'. m, n, k >= 0.
+// With a workspace (work_elems doubles) a GEMM whose output has fewer than kSplitTarget 64x64
+// tiles and K >= 1024 is split along K (deterministic reduction). Without one, nothing is split.
+constexpr long long kSplitTarget = 2 * 152;
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
-           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0);
+           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
+           double *work = nullptr, size_t work_elems = 0);
 
 // Optional timing of every dgemm launch (events around each launch, executed FLOPs counted from
 // the tile k-ranges the kernel actually iterates). Enabled by the context's profiler.
@@ -29,8 +33,10 @@ extern GemmProfile g_gemm_prof;
 // In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
 void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);
 
-// X = L^{-1} for lower-triangular L (X lower, strict upper zero). work: 64*n doubles.
-void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work);
+// X = L^{-1} for lower-triangular L (X lower, strict upper zero). work: >= 64*n doubles (more is
+// used as split-K space).
+void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work,
+                 size_t work_elems);
 
 // Symmetric tridiagonal reduction A = Q T Q^T from the lower triangle of A (n x n, lda).
 // d[n], e[n-1], tau[n-1]; V (n x n, ldv) receives the Householder vectors explicitly
