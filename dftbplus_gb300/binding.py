@@ -34,7 +34,7 @@ class SccOpts(C.Structure):
     _fields_ = [("kT", C.c_double), ("scc_tol", C.c_double), ("max_iter", C.c_int), ("min_iter", C.c_int),
                 ("mix_alpha", C.c_double), ("mix_omega0", C.c_double), ("mix_min_weight", C.c_double),
                 ("mix_max_weight", C.c_double), ("mix_weight_fac", C.c_double), ("net_charge", C.c_double),
-                ("precision", C.c_int), ("convergent_only", C.c_int)]
+                ("precision", C.c_int), ("convergent_only", C.c_int), ("mixed_switch_tol", C.c_double)]
 
 
 class Energies(C.Structure):
@@ -54,6 +54,7 @@ SIGNATURES = {
     "dftbgpu_set_geometry": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip]),
     "dftbgpu_set_geometry_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, _ip]),
     "dftbgpu_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), _dp, C.POINTER(Energies), _dp, _dp, _dp, _dp, _ip, _ip]),
+    "dftbgpu_scc_history": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip, _dp]),
     "dftbgpu_gradients": (C.c_int, [C.c_void_p, _dp]),
     "dftbgpu_gradients_dev": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dftbgpu_n_orbitals": (C.c_int, [C.c_void_p, _ip]),
@@ -71,7 +72,7 @@ SIGNATURES = {
 }
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
-          "density", "mulliken_energy", "broyden", "gradients", "gemm_fp64"]
+          "density", "mulliken_energy", "broyden", "gradients", "gemm_fp64", "gemm_fp32"]
 
 _lib = None
 
@@ -214,6 +215,16 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dftbgpu_kernel_launches(self.h))
+
+    def scc_history(self) -> dict:
+        """Per-iteration record of the last SCC call: electronic energy, SCC error, precision form
+        (PREC_FP64 / PREC_MIXED for an FP32 eigensolve) and host milliseconds."""
+        n = int(self.lib.dftbgpu_scc_history(self.h, 0, None, None, None, None))
+        e, err, ms = np.zeros(n), np.zeros(n), np.zeros(n)
+        prec = np.zeros(n, dtype=np.int32)
+        self.lib.dftbgpu_scc_history(self.h, n, _p(e, C.c_double), _p(err, C.c_double), _p(prec, C.c_int),
+                                     _p(ms, C.c_double))
+        return {"energy": e, "error": err, "precision": prec, "ms": ms}
 
     def profile(self, enable: bool):
         self.check(self.lib.dftbgpu_profile_enable(self.h, 1 if enable else 0))

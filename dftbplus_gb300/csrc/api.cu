@@ -1,6 +1,7 @@
 // C-ABI of the dftbgpu library: context, model/geometry upload, the SCC driver and gradients.
 // Host orchestration only; all numerical work runs in the kernels of linalg.cu, stedc.cu and
 // dftb_kernels.cu on the context's stream.
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -47,6 +48,16 @@ struct Ctx {
          *Z = nullptr, *C = nullptr, *rho = nullptr, *W = nullptr;
   double *Lc = nullptr;   // Cholesky factor of S (lower)
   double *A0 = nullptr;   // L^-1 H0 L^-T (lower), per geometry
+  // FP32 eigensolver buffers of the mixed form (allocated on first use)
+  size_t cap_n32 = 0;
+  float *L32 = nullptr, *Li32 = nullptr, *A0_32 = nullptr, *A32 = nullptr, *T32 = nullptr, *V32 = nullptr,
+        *Z32 = nullptr, *C32 = nullptr, *d32 = nullptr, *e32 = nullptr, *tau32 = nullptr, *wk32_sytrd = nullptr,
+        *wk32_ormtr = nullptr, *wk32_stedc = nullptr;
+  bool mixed_ready = false;
+  int mixed_iters = 0;    // FP32 iterations of the last SCC call
+  // per-iteration record of the last SCC call: electronic energy, max|q_out - q_in|, precision, host ms
+  std::vector<double> hist_e, hist_err, hist_ms;
+  std::vector<int> hist_prec;
   double *eig = nullptr, *fill = nullptr, *fe = nullptr, *dd = nullptr, *ee = nullptr, *tau = nullptr,
          *qorb = nullptr, *eorb = nullptr;
   double *wk_sytrd = nullptr, *wk_ormtr = nullptr, *wk_stedc = nullptr;
@@ -106,14 +117,16 @@ static void flush_marks(Ctx *c) {
     cudaEventSynchronize(gp.ev[i + 1]);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, gp.ev[i], gp.ev[i + 1]);
-    c->prof_ms[kPhGemm] += ms;
-    c->prof_flops[kPhGemm] += gp.flops[i / 2];
-    c->prof_calls[kPhGemm] += 1;
+    const int ph = gp.fp32[i / 2] ? kPhGemm32 : kPhGemm;
+    c->prof_ms[ph] += ms;
+    c->prof_flops[ph] += gp.flops[i / 2];
+    c->prof_calls[ph] += 1;
     cudaEventDestroy(gp.ev[i]);
     cudaEventDestroy(gp.ev[i + 1]);
   }
   gp.ev.clear();
   gp.flops.clear();
+  gp.fp32.clear();
 }
 
 int set_error(Ctx *c, int code, const char *fmt, ...) {
@@ -231,8 +244,8 @@ static int ensure_orbitals(Ctx *c, int n) {
     DG_CHECK(c, dev_alloc(c, p, nn));
   for (double **p : {&c->eig, &c->fill, &c->fe, &c->dd, &c->ee, &c->tau, &c->qorb, &c->eorb})
     DG_CHECK(c, dev_alloc(c, p, (size_t)n));
-  DG_CHECK(c, dev_alloc(c, &c->wk_sytrd, sytrd_work_size(n)));
-  DG_CHECK(c, dev_alloc(c, &c->wk_ormtr, ormtr_work_size(n, n)));
+  DG_CHECK(c, dev_alloc(c, &c->wk_sytrd, sytrd_work_size<double>(n)));
+  DG_CHECK(c, dev_alloc(c, &c->wk_ormtr, ormtr_work_size<double>(n, n)));
   DG_CHECK(c, dev_alloc(c, &c->wk_stedc, stedc_work_size(n)));
   DG_CHECK(c, dev_alloc(c, &c->iwk_stedc, stedc_iwork_size(n)));
   c->cap_n = n;
@@ -252,6 +265,29 @@ static int ensure_broyden(Ctx *c, int natom, int max_iter) {
   c->bro.max_iter = M;
   c->bro_cap_iter = M;
   c->bro_cap_atoms = N;
+  return DFTBGPU_OK;
+}
+
+// FP32 copies of L, L^-1 and A0 for the reduced-precision iterations (once per geometry).
+static int ensure_mixed(Ctx *c, int n) {
+  if ((size_t)n > c->cap_n32) {
+    size_t nn = (size_t)n * n;
+    for (float **p : {&c->L32, &c->Li32, &c->A0_32, &c->A32, &c->T32, &c->V32, &c->Z32, &c->C32})
+      DG_CHECK(c, dev_alloc(c, p, nn));
+    for (float **p : {&c->d32, &c->e32, &c->tau32}) DG_CHECK(c, dev_alloc(c, p, (size_t)n));
+    DG_CHECK(c, dev_alloc(c, &c->wk32_sytrd, sytrd_work_size<float>(n)));
+    DG_CHECK(c, dev_alloc(c, &c->wk32_ormtr, ormtr_work_size<float>(n, n)));
+    DG_CHECK(c, dev_alloc(c, &c->wk32_stedc, stedc_work_size(n)));
+    c->cap_n32 = n;
+    c->mixed_ready = false;
+  }
+  if (!c->mixed_ready) {
+    size_t nn = (size_t)n * n;
+    convert_d2f(c->stream, nn, c->Lc, c->L32);
+    convert_d2f(c->stream, nn, c->Linv, c->Li32);
+    convert_d2f(c->stream, nn, c->A0, c->A0_32);
+    c->mixed_ready = true;
+  }
   return DFTBGPU_OK;
 }
 
@@ -335,6 +371,7 @@ void dftbgpu_default_opts(dftbgpu_scc_opts *o) {
   o->net_charge = 0.0;
   o->precision = DFTBGPU_PREC_FP64;
   o->convergent_only = 0;
+  o->mixed_switch_tol = 0.0;
 }
 
 int dftbgpu_create(dftbgpu_ctx **out, int device) {
@@ -367,7 +404,9 @@ int dftbgpu_destroy(dftbgpu_ctx *c) {
                   c->d_eatom, c->d_grad, c->H0, c->S, c->Linv, c->H, c->T, c->Vh, c->Z, c->C, c->rho,
                   c->W, c->Lc, c->A0, c->eig, c->fill, c->fe, c->dd, c->ee, c->tau, c->qorb, c->eorb, c->wk_sytrd,
                   c->wk_ormtr, c->wk_stedc, c->iwk_stedc, c->d_status, c->d_scal, c->bro.ww, c->bro.aa,
-                  c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast};
+                  c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast, c->L32, c->Li32, c->A0_32, c->A32,
+                  c->T32, c->V32, c->Z32, c->C32, c->d32, c->e32, c->tau32, c->wk32_sytrd, c->wk32_ormtr,
+                  c->wk32_stedc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   cudaStreamDestroy(c->stream);
@@ -546,6 +585,7 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   c->have_geom = true;
   c->have_scc = false;
   c->have_w = false;
+  c->mixed_ready = false;
   return DFTBGPU_OK;
 }
 
@@ -563,7 +603,8 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   if (!c->have_geom) return set_error(c, DFTBGPU_ERR_STATE, "scc: no geometry set");
   if (o->max_iter < 1 || o->max_iter > 150) return set_error(c, DFTBGPU_ERR_ARGS, "scc: max_iter must be in 1..150");
   if (!(o->kT > 0.0)) return set_error(c, DFTBGPU_ERR_ARGS, "scc: kT must be > 0 (Fermi filling)");
-  if (o->precision != DFTBGPU_PREC_FP64) return set_error(c, DFTBGPU_ERR_ARGS, "scc: precision form %d not available", o->precision);
+  if (o->precision != DFTBGPU_PREC_FP64 && o->precision != DFTBGPU_PREC_MIXED)
+    return set_error(c, DFTBGPU_ERR_ARGS, "scc: unknown precision form %d", o->precision);
   cudaSetDevice(c->device);
   cudaStream_t s = c->stream;
   const int n = c->norb, N = c->natom;
@@ -580,46 +621,97 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   double h_scal[kSCount];
   int it = 0;
   bool conv = false;
+  // Mixed form: reduced-precision (FP32) eigensolves until max|q_out - q_in| < switch_tol, then FP64
+  // to convergence (the converged state is always an FP64 iteration).
+  bool low = (o->precision == DFTBGPU_PREC_MIXED);
+  const double switch_tol = (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 1e-4;
+  if (low) DG_CHECK(c, ensure_mixed(c, n));
+  c->mixed_iters = 0;
+  c->hist_e.clear(); c->hist_err.clear(); c->hist_ms.clear(); c->hist_prec.clear();
+  int mix_calls = 0;
+  auto pick = [&](int *kout) -> int {
+    fermi_filling(s, n, c->eig, nel, o->kT, c->fill, c->d_scal);
+    DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
+    DG_CUDA(c, cudaStreamSynchronize(s));
+    int st = 0;
+    DG_CUDA(c, cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "eigensolver: secular iteration cap reached");
+    if (h_scal[kSFermiStatus] != 0.0) return set_error(c, DFTBGPU_ERR_FERMI, "Fermi level search did not converge.");
+    *kout = (int)h_scal[kSNLevels];
+    return DFTBGPU_OK;
+  };
   for (it = 1; it <= o->max_iter; ++it) {
+    const auto t_it = std::chrono::steady_clock::now();
+    const bool it_low = low;
     mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
-    // reduced problem A = L^-1 H L^-T = A0 + 1/2 (B + B^T), B = L^-1 (diag(V) L)
-    mark(c, kPhTransform);
-    prof_flops(c, kPhTransform, (double)n * n * n);
-    reduced_shift(s, g, c->Lc, c->d_V, c->T);
-    dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
-    add_half_lower(s, n, c->A0, c->C, c->H);
     int k = 0;
-    auto pick = [&](int *kout) -> int {
-      fermi_filling(s, n, c->eig, nel, o->kT, c->fill, c->d_scal);
-      DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
-      DG_CUDA(c, cudaStreamSynchronize(s));
-      int st = 0;
-      DG_CUDA(c, cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-      if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "eigensolver: secular iteration cap reached");
-      if (h_scal[kSFermiStatus] != 0.0) return set_error(c, DFTBGPU_ERR_FERMI, "Fermi level search did not converge.");
-      *kout = (int)h_scal[kSNLevels];
-      return DFTBGPU_OK;
-    };
-    DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true));
-    k = (int)h_scal[kSNLevels];
+    if (low) {
+      c->mixed_iters++;
+      mark(c, kPhTransform);
+      reduced_shift_f(s, g, c->L32, c->d_V, c->T32);
+      gemm<float>(s, 'N', 'N', n, n, n, 1.f, c->Li32, n, c->T32, n, 0.f, c->C32, n, kALower | kBLower | kCLower);
+      add_half_lower_f(s, n, c->A0_32, c->C32, c->A32);
+      mark(c, kPhSytrd);
+      sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd);
+      mark(c, kPhStedc);
+      if (stedc<float>(s, n, c->d32, c->e32, c->Z32, n, c->wk32_stedc, c->iwk_stedc, c->d_status) != 0)
+        return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
+      convert_f2d(s, n, c->d32, c->eig);
+      mark(c, kPhFermi);
+      DG_CHECK(c, pick(&k));
+      mark(c, kPhBack);
+      if (k > 0) {
+        ormtr_left<float>(s, n, k, c->V32, n, c->tau32, c->Z32, n, c->wk32_ormtr);
+        gemm<float>(s, 'T', 'N', n, k, n, 1.f, c->Li32, n, c->Z32, n, 0.f, c->C32, n, kAUpper);
+      }
+      mark(c, kPhDensity);
+      if (k > 0) {
+        scale_columns<float>(s, n, k, c->C32, n, c->fill, c->T32, n);
+        gemm<float>(s, 'N', 'T', n, n, k, 1.f, c->T32, n, c->C32, n, 0.f, c->A32, n, kCLower);
+        lower_f_to_sym_d(s, n, c->A32, c->rho);
+      } else {
+        set_zero(s, c->rho, (size_t)n * n);
+      }
+    } else {
+      // reduced problem A = L^-1 H L^-T = A0 + 1/2 (B + B^T), B = L^-1 (diag(V) L)
+      mark(c, kPhTransform);
+      prof_flops(c, kPhTransform, (double)n * n * n);
+      reduced_shift(s, g, c->Lc, c->d_V, c->T);
+      dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
+      add_half_lower(s, n, c->A0, c->C, c->H);
+      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true));
+      k = (int)h_scal[kSNLevels];
+      mark(c, kPhDensity);
+      prof_flops(c, kPhDensity, (double)n * n * k);
+      DG_CHECK(c, density(c, n, k, c->fill, c->rho));
+    }
     c->nlevels = k;
-    mark(c, kPhDensity);
-    prof_flops(c, kPhDensity, (double)n * n * k);
-    DG_CHECK(c, density(c, n, k, c->fill, c->rho));
     mark(c, kPhMulliken);
     mulliken(s, g, c->rho, c->S, c->H0, c->qorb, c->d_qout, c->eorb, c->d_scal);
     potential(s, m, g, c->d_qout, c->d_q0, c->d_Vout);
     scc_energy(s, N, c->d_Vout, c->d_qout, c->d_q0, c->d_scal);
     mark(c, kPhBroyden);
-    broyden_step(s, N, it, o->min_iter, o->max_iter, o->scc_tol, o->mix_alpha, o->mix_omega0, o->mix_min_weight,
-                 o->mix_max_weight, o->mix_weight_fac, c->bro, c->d_qin, c->d_qout, c->d_scal);
+    broyden_step(s, N, it, mix_calls + 1, o->min_iter, o->max_iter, o->scc_tol, o->mix_alpha, o->mix_omega0,
+                 o->mix_min_weight, o->mix_max_weight, o->mix_weight_fac, c->bro, c->d_qin, c->d_qout, c->d_scal);
     mark(c, -1);
     DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
     DG_CUDA(c, cudaGetLastError());
     flush_marks(c);
+    c->hist_e.push_back(h_scal[kSEnonScc] + h_scal[kSEscc]);
+    c->hist_err.push_back(h_scal[kSErr]);
+    c->hist_prec.push_back(it_low ? DFTBGPU_PREC_MIXED : DFTBGPU_PREC_FP64);
+    c->hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_it).count());
     conv = h_scal[kSConv] != 0.0;
+    if (!conv && it != o->max_iter) ++mix_calls;
+    if (low && (conv || h_scal[kSErr] < switch_tol)) {
+      // converged or close enough in reduced precision: finish in FP64 (a converged FP32 state is
+      // re-evaluated, not accepted)
+      low = false;
+      conv = false;
+      continue;
+    }
     if (conv) break;
   }
   if (it > o->max_iter) it = o->max_iter;
@@ -644,6 +736,19 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   if (!conv && o->convergent_only)
     return set_error(c, DFTBGPU_ERR_SCC_NOT_CONVERGED, "SCC is NOT converged, maximal SCC iterations exceeded");
   return DFTBGPU_OK;
+}
+
+int dftbgpu_scc_history(const dftbgpu_ctx *c, int cap, double *energy, double *error, int *precision,
+                        double *ms) {
+  if (!c || cap < 0) return -1;
+  const int n = (int)c->hist_err.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (energy) energy[i] = c->hist_e[i];
+    if (error) error[i] = c->hist_err[i];
+    if (precision) precision[i] = c->hist_prec[i];
+    if (ms) ms[i] = c->hist_ms[i];
+  }
+  return n;
 }
 
 static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {

@@ -456,6 +456,61 @@ void add_half_lower(cudaStream_t s, int n, const double *A0, const double *B, do
   count_launch();
 }
 
+// FP32 counterparts for the reduced-precision SCC iterations of the mixed form.
+__global__ void scale_rows_lower_f_kernel(int n, const int *orb_atom, const float *L, const double *V, float *DL) {
+  int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    size_t idx = i + (size_t)j * n;
+    DL[idx] = (i >= j) ? (float)V[orb_atom[i]] * L[idx] : 0.0f;
+  }
+}
+__global__ void add_half_lower_f_kernel(int n, const float *A0, const float *B, float *A) {
+  int j = blockIdx.y;
+  for (int i = j + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    size_t idx = i + (size_t)j * n;
+    A[idx] = A0[idx] + ((i == j) ? B[idx] : 0.5f * B[idx]);
+  }
+}
+__global__ void d2f_kernel(size_t n, const double *x, float *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+__global__ void f2d_kernel(size_t n, const float *x, double *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+// full symmetric FP64 matrix from the lower triangle of an FP32 one
+__global__ void lower_f_to_sym_d_kernel(int n, const float *A, double *B) {
+  int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    B[i + (size_t)j * n] = (double)((i >= j) ? A[i + (size_t)j * n] : A[j + (size_t)i * n]);
+}
+
+void reduced_shift_f(cudaStream_t s, const GeomDev &g, const float *L, const double *V, float *DL) {
+  const int *orb_atom = g.orb_off + g.natom + 1;
+  dim3 grid(std::min(ceil_div(g.norb, 256), 4), g.norb);
+  scale_rows_lower_f_kernel<<<grid, 256, 0, s>>>(g.norb, orb_atom, L, V, DL);
+  count_launch();
+}
+void add_half_lower_f(cudaStream_t s, int n, const float *A0, const float *B, float *A) {
+  dim3 grid(std::min(ceil_div(n, 256), 4), n);
+  add_half_lower_f_kernel<<<grid, 256, 0, s>>>(n, A0, B, A);
+  count_launch();
+}
+void convert_d2f(cudaStream_t s, size_t n, const double *x, float *y) {
+  d2f_kernel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(n, x, y);
+  count_launch();
+}
+void convert_f2d(cudaStream_t s, size_t n, const float *x, double *y) {
+  f2d_kernel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(n, x, y);
+  count_launch();
+}
+void lower_f_to_sym_d(cudaStream_t s, int n, const float *A, double *B) {
+  dim3 grid(std::min(ceil_div(n, 256), 4), n);
+  lower_f_to_sym_d_kernel<<<grid, 256, 0, s>>>(n, A, B);
+  count_launch();
+}
+
 void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double *S, const double *V,
                 double *H) {
   // orb_off holds natom+1 entries followed by norb orbital->atom entries (see api.cu)
@@ -747,7 +802,8 @@ void repulsive_energy(cudaStream_t s, const ModelDev &m, const GeomDev &g, doubl
 // ------------------------------------------------------------------------------ Broyden
 // mixer/broydenmixer.F90:204-342 (modified Broyden, Johnson 1988) in one CTA. The SCC convergence
 // test max|q_out - q_in| < tol (main.F90:4907-4908) decides whether a mixing step is taken.
-__global__ void __launch_bounds__(1024) broyden_kernel(int N, int it, int min_iter, int max_iter_scc, double tol,
+__global__ void __launch_bounds__(1024) broyden_kernel(int N, int it, int mix_it, int min_iter, int max_iter_scc,
+                                                       double tol,
                                                        double alpha, double omega0, double minw, double maxw,
                                                        double wfac, BroydenDev B, double *qin,
                                                        const double *qout, double *scal) {
@@ -774,7 +830,7 @@ __global__ void __launch_bounds__(1024) broyden_kernel(int N, int it, int min_it
     scal[kSConv] = conv ? 1.0 : 0.0;
   }
   if (conv || it == max_iter_scc) return;
-  const int nn = it;
+  const int nn = mix_it;  // number of this mixing step (the mixer's own counter)
   if (nn > B.max_iter) return;
   auto bsum = [&](double v) -> double {
     v = warp_sum(v);
@@ -906,8 +962,8 @@ __global__ void __launch_bounds__(1024) broyden_kernel(int N, int it, int min_it
   }
 }
 
-void broyden_step(cudaStream_t s, int natom, int it, int min_iter, int max_iter_scc, double tol, double alpha,
-                  double omega0, double minw, double maxw, double wfac, BroydenDev b, double *qin,
+void broyden_step(cudaStream_t s, int natom, int it, int mix_it, int min_iter, int max_iter_scc, double tol,
+                  double alpha, double omega0, double minw, double maxw, double wfac, BroydenDev b, double *qin,
                   const double *qout, double *scal) {
   size_t smem = sizeof(double) * ((size_t)b.max_iter + (size_t)b.max_iter * b.max_iter);
   static bool attr = false;
@@ -915,8 +971,8 @@ void broyden_step(cudaStream_t s, int natom, int it, int min_iter, int max_iter_
     cudaFuncSetAttribute(broyden_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  broyden_kernel<<<1, 1024, smem, s>>>(natom, it, min_iter, max_iter_scc, tol, alpha, omega0, minw, maxw, wfac,
-                                       b, qin, qout, scal);
+  broyden_kernel<<<1, 1024, smem, s>>>(natom, it, mix_it, min_iter, max_iter_scc, tol, alpha, omega0, minw, maxw,
+                                       wfac, b, qin, qout, scal);
   count_launch();
 }
 

@@ -45,6 +45,12 @@ void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double
 void reduced_shift(cudaStream_t s, const GeomDev &g, const double *L, const double *V, double *DL);
 // A(lower) = A0 + 1/2 (B + B^T), B lower triangular
 void add_half_lower(cudaStream_t s, int n, const double *A0, const double *B, double *A);
+// FP32 versions and conversions for the reduced-precision iterations
+void reduced_shift_f(cudaStream_t s, const GeomDev &g, const float *L, const double *V, float *DL);
+void add_half_lower_f(cudaStream_t s, int n, const float *A0, const float *B, float *A);
+void convert_d2f(cudaStream_t s, size_t n, const double *x, float *y);
+void convert_f2d(cudaStream_t s, size_t n, const float *x, double *y);
+void lower_f_to_sym_d(cudaStream_t s, int n, const float *A, double *B);
 // Fermi filling (spin unpolarised) from ascending eigenvalues; writes fill[n], scal[...]
 void fermi_filling(cudaStream_t s, int n, const double *eig, double nel, double kT, double *fill,
                    double *scal);
@@ -58,7 +64,7 @@ struct BroydenDev {
   int max_iter;
   double *ww, *aa, *dF, *uu, *qlast, *dlast;
 };
-void broyden_step(cudaStream_t s, int natom, int it, int min_iter, int max_iter_scc, double tol,
+void broyden_step(cudaStream_t s, int natom, int it, int mix_it, int min_iter, int max_iter_scc, double tol,
                   double alpha, double omega0, double minw, double maxw, double wfac,
                   BroydenDev b, double *qin, const double *qout, double *scal);
 // gradients

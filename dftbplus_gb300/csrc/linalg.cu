@@ -14,15 +14,15 @@ namespace dg {
 // With P != nullptr the CTA (x, y, z) sums only the z-th of gridDim.z slices of its k-range and
 // writes the raw sum to P + z*m*n (split-K; dgemm_splitk_reduce applies alpha/beta in a fixed
 // order, so results stay deterministic).
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double alpha,
-                                                    const double *__restrict__ A, int lda,
-                                                    const double *__restrict__ B, int ldb,
-                                                    double beta, double *__restrict__ C, int ldc,
-                                                    int flags, double *__restrict__ P) {
+template <typename T, bool TA, bool TB>
+__global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, T alpha,
+                                                    const T *__restrict__ A, int lda,
+                                                    const T *__restrict__ B, int ldb,
+                                                    T beta, T *__restrict__ C, int ldc,
+                                                    int flags, T *__restrict__ P) {
   constexpr int BM = 64, BN = 64, BK = 16;
-  __shared__ double As[BK][BM + 1];
-  __shared__ double Bs[BK][BN + 1];
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int i0 = blockIdx.x * BM, j0 = blockIdx.y * BN;
@@ -40,13 +40,13 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
     kmin = lo;
   }
 
-  double acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
-  double ra[4], rb[4];
+  T ra[4], rb[4];
   auto load_a = [&](int p0) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
       int ii, pp;
       if (!TA) { ii = t & 63; pp = t >> 6; } else { pp = t & 15; ii = t >> 4; }
       int gi = i0 + ii, gp = p0 + pp;
-      double v = 0.0;
+      T v = T(0);
       if (gi < m && gp < kmax) v = TA ? A[gp + (size_t)gi * lda] : A[gi + (size_t)gp * lda];
       ra[r] = v;
     }
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
       int pp, jj;
       if (!TB) { pp = t & 15; jj = t >> 4; } else { jj = t & 63; pp = t >> 6; }
       int gj = j0 + jj, gp = p0 + pp;
-      double v = 0.0;
+      T v = T(0);
       if (gj < n && gp < kmax) v = TB ? B[gj + (size_t)gp * ldb] : B[gp + (size_t)gj * ldb];
       rb[r] = v;
     }
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
       }
 #pragma unroll
       for (int pp = 0; pp < BK; ++pp) {
-        double a[4], b[4];
+        T a[4], b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = As[pp][tx + 16 * i];
 #pragma unroll
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
     }
   }
   if (P != nullptr) {
-    double *Pz = P + (size_t)blockIdx.z * m * n;
+    T *Pz = P + (size_t)blockIdx.z * m * n;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       int gi = i0 + tx + 16 * i;
@@ -131,27 +131,28 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int m, int n, int k, double 
     for (int j = 0; j < 4; ++j) {
       int gj = j0 + ty + 16 * j;
       if (gj >= n) continue;
-      double *c = C + gi + (size_t)gj * ldc;
-      double v = alpha * acc[i][j];
-      if (beta != 0.0) v = fma(beta, *c, v);
+      T *c = C + gi + (size_t)gj * ldc;
+      T v = alpha * acc[i][j];
+      if (beta != T(0)) v = fma(beta, *c, v);
       *c = v;
     }
   }
 }
 
 // C = alpha * sum_z P[z] + beta * C over the tiles a split-K dgemm computed.
-__global__ void dgemm_splitk_reduce(int m, int n, int splits, const double *__restrict__ P, double alpha,
-                                    double beta, double *__restrict__ C, int ldc, int flags) {
+template <typename T>
+__global__ void dgemm_splitk_reduce(int m, int n, int splits, const T *__restrict__ P, T alpha,
+                                    T beta, T *__restrict__ C, int ldc, int flags) {
   size_t total = (size_t)m * n;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
     int i = (int)(idx % m), j = (int)(idx / m);
     if ((flags & kCLower) && (i | 63) < (j & ~63)) continue;  // tile skipped by the GEMM
-    double s = 0.0;
+    T s = T(0);
     for (int z = 0; z < splits; ++z) s += P[(size_t)z * total + idx];
-    double *c = C + i + (size_t)j * ldc;
-    double v = alpha * s;
-    if (beta != 0.0) v = fma(beta, *c, v);
+    T *c = C + i + (size_t)j * ldc;
+    T v = alpha * s;
+    if (beta != T(0)) v = fma(beta, *c, v);
     *c = v;
   }
 }
@@ -173,14 +174,17 @@ static double gemm_executed_flops(int m, int n, int k, int flags) {
   return f;
 }
 
-void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
-           int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags, double *work,
-           size_t work_elems) {
+template <typename T>
+void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda, const T *B,
+          int ldb, T beta, T *C, int ldc, int flags, T *work, size_t work_elems) {
   if (m <= 0 || n <= 0) return;
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64));
   bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (g_gemm_prof.on) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
+  const bool prof = g_gemm_prof.on && cap == cudaStreamCaptureStatusNone;
+  if (prof) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
@@ -196,28 +200,40 @@ void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, 
     splits = (int)sp;
     if (splits < 2) splits = 1;
   }
-  double *P = (splits > 1) ? work : nullptr;
+  T *P = (splits > 1) ? work : nullptr;
   grid.z = splits;
   if (!TA && !TB)
-    dgemm_kernel<false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
+    dgemm_kernel<T, false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else if (!TA && TB)
-    dgemm_kernel<false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
+    dgemm_kernel<T, false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else if (TA && !TB)
-    dgemm_kernel<true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
+    dgemm_kernel<T, true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else
-    dgemm_kernel<true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
+    dgemm_kernel<T, true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   count_launch();
   if (P) {
     int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
-    dgemm_splitk_reduce<<<rb, 256, 0, s>>>(m, n, splits, P, alpha, beta, C, ldc, flags);
+    dgemm_splitk_reduce<T><<<rb, 256, 0, s>>>(m, n, splits, P, alpha, beta, C, ldc, flags);
     count_launch();
   }
-  if (g_gemm_prof.on) {
+  if (prof) {
     cudaEventRecord(e1, s);
     g_gemm_prof.ev.push_back(e0);
     g_gemm_prof.ev.push_back(e1);
     g_gemm_prof.flops.push_back(gemm_executed_flops(m, n, k, flags));
+    g_gemm_prof.fp32.push_back(sizeof(T) == 4);
   }
+}
+
+template void gemm<double>(cudaStream_t, char, char, int, int, int, double, const double *, int,
+                           const double *, int, double, double *, int, int, double *, size_t);
+template void gemm<float>(cudaStream_t, char, char, int, int, int, float, const float *, int, const float *,
+                          int, float, float *, int, int, float *, size_t);
+
+void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+           const double *B, int ldb, double beta, double *C, int ldc, int flags, double *work,
+           size_t work_elems) {
+  gemm<double>(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, work, work_elems);
 }
 
 // ------------------------------------------------------------------------------------- helpers
@@ -233,14 +249,15 @@ void set_zero(cudaStream_t s, double *p, size_t n) {
 }
 
 // 32x32 tiles through shared memory so both the read (lower) and the write (upper) are coalesced.
-__global__ void lower_to_upper_kernel(int n, double *A, int lda) {
-  __shared__ double t[32][33];
+template <typename T>
+__global__ void lower_to_upper_kernel(int n, T *A, int lda) {
+  __shared__ T t[32][33];
   int bi = blockIdx.x, bj = blockIdx.y;  // tile (bi, bj) with bi >= bj in the lower triangle
   if (bi < bj) return;
   int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
   for (int r = ty; r < 32; r += 8) {
     int gi = bi * 32 + tx, gj = bj * 32 + r;
-    t[r][tx] = (gi < n && gj < n) ? A[gi + (size_t)gj * lda] : 0.0;
+    t[r][tx] = (gi < n && gj < n) ? A[gi + (size_t)gj * lda] : T(0);
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
@@ -248,11 +265,14 @@ __global__ void lower_to_upper_kernel(int n, double *A, int lda) {
     if (gi < n && gj < n && gj > gi) A[gi + (size_t)gj * lda] = t[tx][r];
   }
 }
-void copy_lower_to_upper(cudaStream_t s, int n, double *A, int lda) {
+template <typename T>
+void copy_lower_to_upper(cudaStream_t s, int n, T *A, int lda) {
   dim3 g(ceil_div(n, 32), ceil_div(n, 32));
-  lower_to_upper_kernel<<<g, dim3(32, 8), 0, s>>>(n, A, lda);
+  lower_to_upper_kernel<T><<<g, dim3(32, 8), 0, s>>>(n, A, lda);
   count_launch();
 }
+template void copy_lower_to_upper<double>(cudaStream_t, int, double *, int);
+template void copy_lower_to_upper<float>(cudaStream_t, int, float *, int);
 
 __global__ void zero_upper_kernel(int n, double *A, int lda) {
   int j = blockIdx.y;
@@ -265,20 +285,37 @@ void zero_strict_upper(cudaStream_t s, int n, double *A, int lda) {
   count_launch();
 }
 
-__global__ void scale_columns_kernel(int m, int n, const double *A, int lda, const double *f, double *B,
-                                     int ldb) {
+template <typename T>
+__global__ void scale_columns_kernel(int m, int n, const T *A, int lda, const double *f, T *B, int ldb) {
   int j = blockIdx.y;
-  double fj = f[j];
+  T fj = (T)f[j];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
     B[i + (size_t)j * ldb] = A[i + (size_t)j * lda] * fj;
 }
-void scale_columns(cudaStream_t s, int m, int n, const double *A, int lda, const double *f, double *B,
-                   int ldb) {
+template <typename T>
+void scale_columns(cudaStream_t s, int m, int n, const T *A, int lda, const double *f, T *B, int ldb) {
   if (m <= 0 || n <= 0) return;
   dim3 g(std::min(ceil_div(m, 256), 8), n);
-  scale_columns_kernel<<<g, 256, 0, s>>>(m, n, A, lda, f, B, ldb);
+  scale_columns_kernel<T><<<g, 256, 0, s>>>(m, n, A, lda, f, B, ldb);
   count_launch();
 }
+template void scale_columns<double>(cudaStream_t, int, int, const double *, int, const double *, double *, int);
+template void scale_columns<float>(cudaStream_t, int, int, const float *, int, const double *, float *, int);
+
+template <typename T>
+__global__ void set_zero_t_kernel(T *p, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = T(0);
+}
+template <typename T>
+void set_zero_t(cudaStream_t s, T *p, size_t n) {
+  if (!n) return;
+  int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  set_zero_t_kernel<T><<<blocks, 256, 0, s>>>(p, n);
+  count_launch();
+}
+template void set_zero_t<float>(cudaStream_t, float *, size_t);
+template void set_zero_t<double>(cudaStream_t, double *, size_t);
 
 // ------------------------------------------------------------------------------------- Cholesky
 constexpr int NB = 64;
@@ -413,21 +450,22 @@ constexpr int PB = 32;
 constexpr int ST = 64;        // symv tile
 constexpr int RED_THREADS = 1024;
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-template <int NT>
-__device__ double block_sum(double v, double *sh) {
+template <int NT, typename T>
+__device__ T block_sum(T v, T *sh) {
   v = warp_sum(v);
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) sh[w] = v;
   __syncthreads();
-  double r = 0.0;
+  T r = T(0);
   if (threadIdx.x < 32) {
-    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : 0.0;
+    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : T(0);
     r = warp_sum(r);
     if (threadIdx.x == 0) sh[0] = r;
   }
@@ -439,21 +477,22 @@ __device__ double block_sum(double v, double *sh) {
 
 // Step 1a of column j (grid over rows): apply the panel's previous reflectors to A(j:n, j) and
 // write per-CTA partial sums of squares of A(j+2:n, j).
-__global__ void __launch_bounds__(256) latrd_update_kernel(int n, int j, int jj, double *A, int lda,
-                                                           const double *Vp, const double *Wp,
-                                                           double *part) {
-  __shared__ double sh[32];
-  __shared__ double coef[2 * PB];
+template <typename T>
+__global__ void __launch_bounds__(256) latrd_update_kernel(int n, int j, int jj, T *A, int lda,
+                                                           const T *Vp, const T *Wp,
+                                                           T *part) {
+  __shared__ T sh[32];
+  __shared__ T coef[2 * PB];
   const int t = threadIdx.x;
   if (t < jj) {
     coef[t] = Wp[j + (size_t)t * n];        // W(j, q)
     coef[PB + t] = Vp[j + (size_t)t * n];   // V(j, q)
   }
   __syncthreads();
-  double *col = A + (size_t)j * lda;
-  double sig = 0.0;
+  T *col = A + (size_t)j * lda;
+  T sig = T(0);
   for (int r = j + blockIdx.x * blockDim.x + t; r < n; r += gridDim.x * blockDim.x) {
-    double a = col[r];
+    T a = col[r];
     for (int q = 0; q < jj; ++q)
       a -= Vp[r + (size_t)q * n] * coef[q] + Wp[r + (size_t)q * n] * coef[PB + q];
     col[r] = a;
@@ -465,25 +504,26 @@ __global__ void __launch_bounds__(256) latrd_update_kernel(int n, int j, int jj,
 
 // Step 1b (grid over rows): every CTA forms the same reflector from the partial sums (dlarfg
 // semantics: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta) and writes its rows of v.
-__global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, const double *A, int lda,
-                                                          const double *part, int nparts, double *Vp,
-                                                          double *V, int ldv, double *d, double *e,
-                                                          double *tau) {
-  __shared__ double s_scale;
-  const double *col = A + (size_t)j * lda;
+template <typename T>
+__global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, const T *A, int lda,
+                                                          const T *part, int nparts, T *Vp,
+                                                          T *V, int ldv, T *d, T *e,
+                                                          T *tau) {
+  __shared__ T s_scale;
+  const T *col = A + (size_t)j * lda;
   if (threadIdx.x == 0) {
-    double sig = 0.0;
+    T sig = T(0);
     for (int i = 0; i < nparts; ++i) sig += part[i];
-    double alpha = col[j + 1];
-    double beta, tv, scale;
-    if (sig == 0.0) {
-      tv = 0.0;
+    T alpha = col[j + 1];
+    T beta, tv, scale;
+    if (sig == T(0)) {
+      tv = T(0);
       beta = alpha;
-      scale = 0.0;
+      scale = T(0);
     } else {
       beta = -copysign(sqrt(alpha * alpha + sig), alpha);
       tv = (beta - alpha) / beta;
-      scale = 1.0 / (alpha - beta);
+      scale = T(1) / (alpha - beta);
     }
     s_scale = scale;
     if (blockIdx.x == 0) {
@@ -493,11 +533,11 @@ __global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, 
     }
   }
   __syncthreads();
-  const double scale = s_scale;
+  const T scale = s_scale;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    double v;
-    if (r <= j) v = 0.0;
-    else if (r == j + 1) v = 1.0;
+    T v;
+    if (r <= j) v = T(0);
+    else if (r == j + 1) v = T(1);
     else v = col[r] * scale;
     Vp[r + (size_t)jj * n] = v;
     V[r + (size_t)j * ldv] = v;
@@ -506,10 +546,11 @@ __global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, 
 
 // y(j+1:n) = A22 v with A22 = A(j+1:n, j+1:n) read from its lower triangle only; partial sums per
 // 64x64 tile pair are reduced deterministically by symv_reduce_kernel.
-__global__ void __launch_bounds__(256) symv_partial_kernel(int m, int T, const double *A22, int lda,
-                                                           const double *v, double *P) {
-  __shared__ double tile[ST][ST + 1];
-  __shared__ double vr[ST], vc[ST];
+template <typename T>
+__global__ void __launch_bounds__(256) symv_partial_kernel(int m, int ntile, const T *A22, int lda,
+                                                           const T *v, T *P) {
+  __shared__ T tile[ST][ST + 1];
+  __shared__ T vr[ST], vc[ST];
   // decode lower tile index -> (r, c), c <= r
   int idx = blockIdx.x;
   int r = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
@@ -521,16 +562,16 @@ __global__ void __launch_bounds__(256) symv_partial_kernel(int m, int T, const d
   for (int k = t; k < ST * ST; k += 256) {
     int ii = k % ST, jj = k / ST;
     int gi = ri0 + ii, gj = ci0 + jj;
-    double a = 0.0;
+    T a = T(0);
     if (gi < m && gj < m) {
-      if (r == c && ii < jj) a = 0.0;  // filled by mirroring below
+      if (r == c && ii < jj) a = T(0);  // filled by mirroring below
       else a = A22[gi + (size_t)gj * lda];
     }
     tile[ii][jj] = a;
   }
   if (t < ST) {
-    vr[t] = (ri0 + t < m) ? v[ri0 + t] : 0.0;
-    vc[t] = (ci0 + t < m) ? v[ci0 + t] : 0.0;
+    vr[t] = (ri0 + t < m) ? v[ri0 + t] : T(0);
+    vc[t] = (ci0 + t < m) ? v[ci0 + t] : T(0);
   }
   __syncthreads();
   if (r == c) {
@@ -543,61 +584,64 @@ __global__ void __launch_bounds__(256) symv_partial_kernel(int m, int T, const d
   // rows: 4 threads per row, each 16 columns
   {
     int row = t >> 2, part = t & 3;
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int q = 0; q < 16; ++q) s = fma(tile[row][part * 16 + q], vc[part * 16 + q], s);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)r * T + c) * ST + row] = s;
+    if (part == 0) P[((size_t)r * ntile + c) * ST + row] = s;
   }
   if (c < r) {
     int colq = t >> 2, part = t & 3;
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int q = 0; q < 16; ++q) s = fma(tile[part * 16 + q][colq], vr[part * 16 + q], s);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)c * T + r) * ST + colq] = s;
+    if (part == 0) P[((size_t)c * ntile + r) * ST + colq] = s;
   }
 }
 
-__global__ void symv_reduce_kernel(int m, int T, const double *P, double *y) {
+template <typename T>
+__global__ void symv_reduce_kernel(int m, int ntile, const T *P, T *y) {
   int r = blockIdx.x, i = threadIdx.x;
   if (r * ST + i >= m) return;
-  double s = 0.0;
-  for (int c = 0; c < T; ++c) s += P[((size_t)r * T + c) * ST + i];
+  T s = T(0);
+  for (int c = 0; c < ntile; ++c) s += P[((size_t)r * ntile + c) * ST + i];
   y[r * ST + i] = s;
 }
 
 // dots[q] = W(:,q)^T v, dots[PB+q] = V(:,q)^T v over rows j+1..n-1 (one CTA per dot).
-__global__ void latrd_dots_kernel(int n, int j, int jj, const double *Vp, const double *Wp, double *dots) {
-  __shared__ double sh[32];
+template <typename T>
+__global__ void latrd_dots_kernel(int n, int j, int jj, const T *Vp, const T *Wp, T *dots) {
+  __shared__ T sh[32];
   int q = blockIdx.x % jj;
   bool isV = blockIdx.x >= jj;
-  const double *X = (isV ? Vp : Wp) + (size_t)q * n;
-  const double *v = Vp + (size_t)jj * n;
-  double s = 0.0;
+  const T *X = (isV ? Vp : Wp) + (size_t)q * n;
+  const T *v = Vp + (size_t)jj * n;
+  T s = T(0);
   for (int r = j + 1 + threadIdx.x; r < n; r += 256) s = fma(X[r], v[r], s);
   s = block_sum<256>(s, sh);
   if (threadIdx.x == 0) dots[(isV ? PB : 0) + q] = s;
 }
 
 // w = tau (y - V (W^T v) - W (V^T v)); partial sums of w^T v per CTA.
-__global__ void latrd_w_kernel(int n, int j, int jj, const double *Vp, double *Wp, const double *y,
-                               const double *dots, const double *tau, double *part) {
-  __shared__ double sh[32];
-  __shared__ double cf[2 * PB];
+template <typename T>
+__global__ void latrd_w_kernel(int n, int j, int jj, const T *Vp, T *Wp, const T *y,
+                               const T *dots, const T *tau, T *part) {
+  __shared__ T sh[32];
+  __shared__ T cf[2 * PB];
   if (threadIdx.x < jj) {
     cf[threadIdx.x] = dots[threadIdx.x];
     cf[PB + threadIdx.x] = dots[PB + threadIdx.x];
   }
   __syncthreads();
-  const double tv = tau[j];
-  const double *v = Vp + (size_t)jj * n;
-  double *w = Wp + (size_t)jj * n;
-  double s = 0.0;
+  const T tv = tau[j];
+  const T *v = Vp + (size_t)jj * n;
+  T *w = Wp + (size_t)jj * n;
+  T s = T(0);
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    double val = 0.0;
+    T val = T(0);
     if (r > j) {
       val = y[r];
       for (int q = 0; q < jj; ++q)
@@ -611,43 +655,46 @@ __global__ void latrd_w_kernel(int n, int j, int jj, const double *Vp, double *W
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-__global__ void latrd_w2_kernel(int n, int j, int jj, const double *Vp, double *Wp, const double *tau,
-                                const double *part, int nparts) {
-  __shared__ double alpha;
+template <typename T>
+__global__ void latrd_w2_kernel(int n, int j, int jj, const T *Vp, T *Wp, const T *tau,
+                                const T *part, int nparts) {
+  __shared__ T alpha;
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    T s = T(0);
     for (int i = 0; i < nparts; ++i) s += part[i];
-    alpha = -0.5 * tau[j] * s;
+    alpha = T(-0.5) * tau[j] * s;
   }
   __syncthreads();
-  const double *v = Vp + (size_t)jj * n;
-  double *w = Wp + (size_t)jj * n;
-  double a = alpha;
+  const T *v = Vp + (size_t)jj * n;
+  T *w = Wp + (size_t)jj * n;
+  T a = alpha;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
     if (r > j) w[r] = fma(a, v[r], w[r]);
 }
 
-__global__ void copy_last_diag_kernel(int n, const double *A, int lda, double *d) {
+template <typename T>
+__global__ void copy_last_diag_kernel(int n, const T *A, int lda, T *d) {
   d[n - 1] = A[(n - 1) + (size_t)(n - 1) * lda];
 }
 
+template <typename T>
 size_t sytrd_work_size(int n) {
-  size_t T = (size_t)ceil_div(n, ST);
-  return 2 * (size_t)n * PB + (size_t)n + T * T * ST + 2 * PB + 1024;
+  size_t nt = (size_t)ceil_div(n, ST);
+  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 1024;
 }
 
-void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e, double *tau, double *V,
-                 int ldv, double *work) {
-  double *Vp = work;
-  double *Wp = Vp + (size_t)n * PB;
-  double *y = Wp + (size_t)n * PB;
-  double *P = y + n;
+template <typename T>
+void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work) {
+  T *Vp = work;
+  T *Wp = Vp + (size_t)n * PB;
+  T *y = Wp + (size_t)n * PB;
+  T *P = y + n;
   size_t T0 = (size_t)ceil_div(n, ST);
-  double *dots = P + T0 * T0 * ST;
-  double *part = dots + 2 * PB;
-  set_zero(s, V, (size_t)ldv * n);
+  T *dots = P + T0 * T0 * ST;
+  T *part = dots + 2 * PB;
+  set_zero_t<T>(s, V, (size_t)ldv * n);
   if (n == 1) {
-    copy_last_diag_kernel<<<1, 1, 0, s>>>(n, A, lda, d);
+    copy_last_diag_kernel<T><<<1, 1, 0, s>>>(n, A, lda, d);
     count_launch();
     return;
   }
@@ -657,32 +704,32 @@ void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e
     for (int jj = 0; jj < nbp; ++jj) {
       int j = p0 + jj;
       const int cb = std::min(ceil_div(n - j, 256), 64);
-      latrd_update_kernel<<<cb, 256, 0, s>>>(n, j, jj, A, lda, Vp, Wp, part);
-      latrd_house_kernel<<<cb, 256, 0, s>>>(n, j, jj, A, lda, part, cb, Vp, V, ldv, d, e, tau);
+      latrd_update_kernel<T><<<cb, 256, 0, s>>>(n, j, jj, A, lda, Vp, Wp, part);
+      latrd_house_kernel<T><<<cb, 256, 0, s>>>(n, j, jj, A, lda, part, cb, Vp, V, ldv, d, e, tau);
       count_launch(2);
       int m = n - j - 1;
-      int T = ceil_div(m, ST);
-      const double *A22 = A + (j + 1) + (size_t)(j + 1) * lda;
-      symv_partial_kernel<<<T * (T + 1) / 2, 256, 0, s>>>(m, T, A22, lda, Vp + (size_t)jj * n + j + 1, P);
-      symv_reduce_kernel<<<T, ST, 0, s>>>(m, T, P, y + j + 1);
+      int nt = ceil_div(m, ST);
+      const T *A22 = A + (j + 1) + (size_t)(j + 1) * lda;
+      symv_partial_kernel<T><<<nt * (nt + 1) / 2, 256, 0, s>>>(m, nt, A22, lda, Vp + (size_t)jj * n + j + 1, P);
+      symv_reduce_kernel<T><<<nt, ST, 0, s>>>(m, nt, P, y + j + 1);
       count_launch(3);
       if (jj > 0) {
-        latrd_dots_kernel<<<2 * jj, 256, 0, s>>>(n, j, jj, Vp, Wp, dots);
+        latrd_dots_kernel<T><<<2 * jj, 256, 0, s>>>(n, j, jj, Vp, Wp, dots);
         count_launch();
       }
-      latrd_w_kernel<<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, y, dots, tau, part);
-      latrd_w2_kernel<<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, tau, part, wblocks);
+      latrd_w_kernel<T><<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, y, dots, tau, part);
+      latrd_w2_kernel<T><<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, tau, part, wblocks);
       count_launch(2);
     }
     int t0 = p0 + nbp;
     int m2 = n - t0;
     if (m2 > 0) {
-      double *At = A + t0 + (size_t)t0 * lda;
-      dgemm(s, 'N', 'T', m2, m2, nbp, -1.0, Vp + t0, n, Wp + t0, n, 1.0, At, lda, kCLower);
-      dgemm(s, 'N', 'T', m2, m2, nbp, -1.0, Wp + t0, n, Vp + t0, n, 1.0, At, lda, kCLower);
+      T *At = A + t0 + (size_t)t0 * lda;
+      gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Vp + t0, n, Wp + t0, n, T(1), At, lda, kCLower);
+      gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Wp + t0, n, Vp + t0, n, T(1), At, lda, kCLower);
     }
   }
-  copy_last_diag_kernel<<<1, 1, 0, s>>>(n, A, lda, d);
+  copy_last_diag_kernel<T><<<1, 1, 0, s>>>(n, A, lda, d);
   count_launch();
 }
 
@@ -690,15 +737,16 @@ void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e
 constexpr int OB = 64;
 
 // T (nb x nb, upper) of the compact WY form: H_p..H_{p+nb-1} = I - V T V^T, from G = V^T V.
-__global__ void larft_kernel(int nb, const double *G, const double *tau, double *T) {
-  __shared__ double t[OB][OB + 1];
+template <typename T>
+__global__ void larft_kernel(int nb, const T *G, const T *tau, T *Tf) {
+  __shared__ T t[OB][OB + 1];
   const int tid = threadIdx.x;
-  for (int k = tid; k < OB * OB; k += blockDim.x) t[k % OB][k / OB] = 0.0;
+  for (int k = tid; k < OB * OB; k += blockDim.x) t[k % OB][k / OB] = T(0);
   __syncthreads();
   for (int i = 0; i < nb; ++i) {
     // t(0:i, i) = -tau_i * T(0:i, 0:i) * G(0:i, i)
-    double ti = tau[i];
-    double v = 0.0;
+    T ti = tau[i];
+    T v = T(0);
     if (tid < i) {
       for (int q = tid; q < i; ++q) v = fma(t[tid][q], G[q + (size_t)i * nb], v);
       v *= -ti;
@@ -708,22 +756,23 @@ __global__ void larft_kernel(int nb, const double *G, const double *tau, double 
     if (tid == 0) t[i][i] = ti;
     __syncthreads();
   }
-  for (int k = tid; k < nb * nb; k += blockDim.x) T[k] = t[k % nb][k / nb];
+  for (int k = tid; k < nb * nb; k += blockDim.x) Tf[k] = t[k % nb][k / nb];
 }
 
+template <typename T>
 size_t ormtr_work_size(int n, int k) {
   // G, T, M, M2 + split-K partials (up to 8 slices of the larger of OB x k and OB x OB)
   return 2 * (size_t)OB * OB + 2 * (size_t)OB * std::max(k, 1) + 8 * (size_t)OB * std::max(k, OB);
 }
 
-void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const double *tau, double *Z,
-                int ldz, double *work) {
+template <typename T>
+void ormtr_left(cudaStream_t s, int n, int k, const T *V, int ldv, const T *tau, T *Z, int ldz, T *work) {
   if (n <= 1 || k <= 0) return;
-  double *G = work;
-  double *T = G + OB * OB;
-  double *M = T + OB * OB;
-  double *M2 = M + (size_t)OB * k;
-  double *SP = M2 + (size_t)OB * k;
+  T *G = work;
+  T *Tf = G + OB * OB;
+  T *M = Tf + OB * OB;
+  T *M2 = M + (size_t)OB * k;
+  T *SP = M2 + (size_t)OB * k;
   const size_t sp_elems = 8 * (size_t)OB * std::max(k, OB);
   int nref = n - 1;  // reflectors j = 0 .. n-2
   int last = ((nref - 1) / OB) * OB;
@@ -731,14 +780,25 @@ void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const do
     int nb = std::min(OB, nref - p0);
     int r0 = p0 + 1;          // first nonzero row of the block's vectors
     int mr = n - r0;
-    const double *Vb = V + r0 + (size_t)p0 * ldv;
-    dgemm(s, 'T', 'N', nb, nb, mr, 1.0, Vb, ldv, Vb, ldv, 0.0, G, nb, 0, SP, sp_elems);
-    larft_kernel<<<1, OB, 0, s>>>(nb, G, tau + p0, T);
+    const T *Vb = V + r0 + (size_t)p0 * ldv;
+    gemm<T>(s, 'T', 'N', nb, nb, mr, T(1), Vb, ldv, Vb, ldv, T(0), G, nb, 0, SP, sp_elems);
+    larft_kernel<T><<<1, OB, 0, s>>>(nb, G, tau + p0, Tf);
     count_launch();
-    dgemm(s, 'T', 'N', nb, k, mr, 1.0, Vb, ldv, Z + r0, ldz, 0.0, M, nb, 0, SP, sp_elems);
-    dgemm(s, 'N', 'N', nb, k, nb, 1.0, T, nb, M, nb, 0.0, M2, nb, kAUpper);
-    dgemm(s, 'N', 'N', mr, k, nb, -1.0, Vb, ldv, M2, nb, 1.0, Z + r0, ldz);
+    gemm<T>(s, 'T', 'N', nb, k, mr, T(1), Vb, ldv, Z + r0, ldz, T(0), M, nb, 0, SP, sp_elems);
+    gemm<T>(s, 'N', 'N', nb, k, nb, T(1), Tf, nb, M, nb, T(0), M2, nb, kAUpper);
+    gemm<T>(s, 'N', 'N', mr, k, nb, T(-1), Vb, ldv, M2, nb, T(1), Z + r0, ldz);
   }
 }
+
+template size_t sytrd_work_size<double>(int);
+template size_t sytrd_work_size<float>(int);
+template void sytrd_lower<double>(cudaStream_t, int, double *, int, double *, double *, double *, double *, int,
+                                  double *);
+template void sytrd_lower<float>(cudaStream_t, int, float *, int, float *, float *, float *, float *, int, float *);
+template size_t ormtr_work_size<double>(int, int);
+template size_t ormtr_work_size<float>(int, int);
+template void ormtr_left<double>(cudaStream_t, int, int, const double *, int, const double *, double *, int,
+                                 double *);
+template void ormtr_left<float>(cudaStream_t, int, int, const float *, int, const float *, float *, int, float *);
 
 }  // namespace dg

@@ -1,10 +1,12 @@
-// FP64 dense linear algebra on one GB300 (column-major, device pointers, one stream).
+// Dense linear algebra on one GB300 (column-major, device pointers, one stream). The eigensolver
+// pieces are templates on the scalar type: FP64 for the plain path, FP32 for the reduced-precision
+// SCC iterations of the mixed form. Cholesky and L^-1 are FP64 only.
 #pragma once
 #include "common.cuh"
 
 namespace dg {
 
-// Triangular structure hints for dgemm (zero regions are skipped, not read).
+// Triangular structure hints for GEMM (zero regions are skipped, not read).
 enum GemmFlags : int {
   kALower = 1,   // op(A)[i][p] == 0 for p > i
   kAUpper = 2,   // op(A)[i][p] == 0 for p < i
@@ -14,19 +16,24 @@ enum GemmFlags : int {
 };
 
 // C = alpha * op(A) * op(B) + beta * C ; op = 'N' or 'T'. m, n, k >= 0.
-// With a workspace (work_elems doubles) a GEMM whose output has fewer than kSplitTarget 64x64
+// With a workspace (work_elems elements) a GEMM whose output has fewer than kSplitTarget 64x64
 // tiles and K >= 1024 is split along K (deterministic reduction). Without one, nothing is split.
 constexpr long long kSplitTarget = 2 * 152;
+template <typename T>
+void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda, const T *B,
+          int ldb, T beta, T *C, int ldc, int flags = 0, T *work = nullptr, size_t work_elems = 0);
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
            double *work = nullptr, size_t work_elems = 0);
 
-// Optional timing of every dgemm launch (events around each launch, executed FLOPs counted from
-// the tile k-ranges the kernel actually iterates). Enabled by the context's profiler.
+// Optional timing of every GEMM launch (events around each launch, executed FLOPs counted from
+// the tile k-ranges the kernel actually iterates). Enabled by the context's profiler; launches
+// recorded into a CUDA graph are not timed individually.
 struct GemmProfile {
   bool on = false;
   std::vector<cudaEvent_t> ev;     // pairs (start, stop)
   std::vector<double> flops;       // per pair
+  std::vector<bool> fp32;          // per pair: FP32 instead of FP64
 };
 extern GemmProfile g_gemm_prof;
 
@@ -40,28 +47,34 @@ void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int
 
 // Symmetric tridiagonal reduction A = Q T Q^T from the lower triangle of A (n x n, lda).
 // d[n], e[n-1], tau[n-1]; V (n x n, ldv) receives the Householder vectors explicitly
-// (column j: zeros for rows <= j, 1 at row j+1). work: see sytrd_work_size().
+// (column j: zeros for rows <= j, 1 at row j+1). work: sytrd_work_size<T>(n) elements.
+template <typename T>
 size_t sytrd_work_size(int n);
-void sytrd_lower(cudaStream_t s, int n, double *A, int lda, double *d, double *e, double *tau,
-                 double *V, int ldv, double *work);
+template <typename T>
+void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work);
 
-// Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: see ormtr_work_size().
+// Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: ormtr_work_size<T>(n, k).
+template <typename T>
 size_t ormtr_work_size(int n, int k);
-void ormtr_left(cudaStream_t s, int n, int k, const double *V, int ldv, const double *tau, double *Z,
-                int ldz, double *work);
+template <typename T>
+void ormtr_left(cudaStream_t s, int n, int k, const T *V, int ldv, const T *tau, T *Z, int ldz, T *work);
 
 // Symmetric tridiagonal eigensolver (divide and conquer): d[n] (in: diagonal, out: eigenvalues
-// ascending), e[n-1] off-diagonal (destroyed); Q (n x n, ldq) eigenvectors. work sizes below.
+// ascending), e[n-1] off-diagonal (read only); Q (n x n, ldq = n) eigenvectors.
+// work: stedc_work_size(n) elements of T, iwork: stedc_iwork_size(n) ints.
 size_t stedc_work_size(int n);
 size_t stedc_iwork_size(int n);
-int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, double *work,
-          int *iwork, int *status_dev);
+template <typename T>
+int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork, int *status_dev);
 
 // Small helpers
 void set_zero(cudaStream_t s, double *p, size_t n);
-void copy_lower_to_upper(cudaStream_t s, int n, double *A, int lda);
+template <typename T>
+void set_zero_t(cudaStream_t s, T *p, size_t n);
+template <typename T>
+void copy_lower_to_upper(cudaStream_t s, int n, T *A, int lda);
 void zero_strict_upper(cudaStream_t s, int n, double *A, int lda);
-void scale_columns(cudaStream_t s, int m, int n, const double *A, int lda, const double *f,
-                   double *B, int ldb);
+template <typename T>
+void scale_columns(cudaStream_t s, int m, int n, const T *A, int lda, const double *f, T *B, int ldb);
 
 }  // namespace dg

@@ -18,7 +18,6 @@
 
 namespace dg {
 
-constexpr double kEps = 2.220446049250313e-16;
 constexpr int kSecularMaxIter = 100;
 constexpr int kSmallMerge = 128;   // merges up to this size use the batched in-CTA product
 
@@ -27,18 +26,36 @@ struct Merge {
   int pad;
 };
 
+template <typename T>
 struct DcWork {
-  double *Ds, *zs, *dl, *w, *tau, *lam, *zh, *rot_cs, *vals;
+  T *Ds, *zs, *dl, *w, *tau, *lam, *zh, *rot_cs, *vals;
   int *perm, *ndpos, *dfpos, *org, *rot_cols, *mK, *mRot, *srcinfo;
-  double *Gs, *U, *Qtmp, *Qalt;
+  T *Gs, *U, *Qtmp, *Qalt;
 };
 
-__device__ __forceinline__ double wsum(double v) {
+// Scalar-type traits: unit roundoff and the range kept by the exponent-tracked products.
+template <typename T> struct Lim;
+template <> struct Lim<double> {
+  static constexpr double eps = 2.220446049250313e-16, big = 1e150, small = 1e-150;
+};
+template <> struct Lim<float> {
+  static constexpr float eps = 1.1920929e-07f, big = 1e30f, small = 1e-30f;
+};
+__device__ __forceinline__ double t_frexp(double x, int *e) { return frexp(x, e); }
+__device__ __forceinline__ float t_frexp(float x, int *e) { return frexpf(x, e); }
+__device__ __forceinline__ double t_ldexp(double x, int e) { return ldexp(x, e); }
+__device__ __forceinline__ float t_ldexp(float x, int e) { return ldexpf(x, e); }
+__device__ __forceinline__ double t_hypot(double x, double y) { return hypot(x, y); }
+__device__ __forceinline__ float t_hypot(float x, float y) { return hypotf(x, y); }
+
+template <typename T>
+__device__ __forceinline__ T wsum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ double wmax(double v) {
+template <typename T>
+__device__ __forceinline__ T wmax(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
@@ -47,32 +64,35 @@ __device__ __forceinline__ double wmax(double v) {
 // Tear: d[m-1] -= |e[m-1]|, d[m] -= |e[m-1]| for every block boundary m. Leaves are single
 // elements, so every m in 1..n-1 is a boundary and each diagonal entry loses both neighbours'
 // couplings (one thread per entry: adjacent boundaries share an entry).
-__global__ void dc_tear_kernel(int n, double *d, const double *e) {
+template <typename T>
+__global__ void dc_tear_kernel(int n, T *d, const T *e) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double v = d[i];
+  T v = d[i];
   if (i > 0) v -= fabs(e[i - 1]);
   if (i < n - 1) v -= fabs(e[i]);
   d[i] = v;
 }
 
-__global__ void dc_identity_kernel(int n, double *Q, int ldq) {
+template <typename T>
+__global__ void dc_identity_kernel(int n, T *Q, int ldq) {
   int j = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    Q[i + (size_t)j * ldq] = (i == j) ? 1.0 : 0.0;
+    Q[i + (size_t)j * ldq] = (i == j) ? T(1) : T(0);
 }
 
 // K1: merge-sort the two eigenvalue lists and form z.
-__global__ void dc_sort_kernel(const Merge *merges, const double *d, const double *e, const double *Q,
-                               int ldq, DcWork W) {
+template <typename T>
+__global__ void dc_sort_kernel(const Merge *merges, const T *d, const T *e, const T *Q,
+                               int ldq, DcWork<T> W) {
   Merge mg = merges[blockIdx.x];
   if (mg.m == mg.b) return;
   const int a = mg.a, m = mg.m, b = mg.b;
   const int nL = m - a, nR = b - m;
-  const double sgn = (e[m - 1] >= 0.0) ? 1.0 : -1.0;
-  const double is2 = 0.70710678118654752440;
+  const T sgn = (e[m - 1] >= T(0)) ? T(1) : T(-1);
+  const T is2 = T(0.70710678118654752440);
   for (int i = threadIdx.x; i < nL + nR; i += blockDim.x) {
-    double val, zv;
+    T val, zv;
     int pos, blk;
     if (i < nL) {
       val = d[a + i];
@@ -103,7 +123,8 @@ __global__ void dc_sort_kernel(const Merge *merges, const double *d, const doubl
 }
 
 // K2: deflation (sequential scan by one thread after a parallel max reduction).
-__global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W) {
+template <typename T>
+__global__ void dc_deflate_kernel(const Merge *merges, const T *e, DcWork<T> W) {
   const int mi = blockIdx.x;
   Merge mg = merges[mi];
   if (mg.m == mg.b) {
@@ -111,8 +132,8 @@ __global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W
     return;
   }
   const int a = mg.a, N = mg.b - mg.a;
-  __shared__ double smax[2][32];
-  double md = 0.0, mz = 0.0;
+  __shared__ T smax[2][32];
+  T md = T(0), mz = T(0);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     md = fmax(md, fabs(W.Ds[a + i]));
     mz = fmax(mz, fabs(W.zs[a + i]));
@@ -129,9 +150,9 @@ __global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W
   }
   md = fmax(md, smax[0][0]);
   mz = fmax(mz, smax[1][0]);
-  const double rho2 = 2.0 * fabs(e[mg.m - 1]);
-  const double tol = 8.0 * kEps * fmax(md, mz);
-  double *Ds = W.Ds + a, *zs = W.zs + a;
+  const T rho2 = T(2) * fabs(e[mg.m - 1]);
+  const T tol = T(8) * Lim<T>::eps * fmax(md, mz);
+  T *Ds = W.Ds + a, *zs = W.zs + a;
   int *perm = W.perm + a;
   int nrot = 0, K = 0, nD = 0;
   // flags are kept in ndpos temporarily: 1 = deflated
@@ -147,20 +168,20 @@ __global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W
         continue;
       }
       if (prev >= 0) {
-        double s = zs[prev], c = zs[j];
-        double t = hypot(c, s);
-        double tdiff = Ds[j] - Ds[prev];
+        T s = zs[prev], c = zs[j];
+        T t = t_hypot(c, s);
+        T tdiff = Ds[j] - Ds[prev];
         c /= t;
         s = -s / t;
         if (fabs(tdiff * c * s) <= tol) {
           zs[j] = t;
-          zs[prev] = 0.0;
+          zs[prev] = T(0);
           W.rot_cols[2 * (a + nrot)] = a + perm[prev];
           W.rot_cols[2 * (a + nrot) + 1] = a + perm[j];
           W.rot_cs[2 * (a + nrot)] = c;
           W.rot_cs[2 * (a + nrot) + 1] = s;
           ++nrot;
-          double tt = Ds[prev] * c * c + Ds[j] * s * s;
+          T tt = Ds[prev] * c * c + Ds[j] * s * s;
           Ds[j] = Ds[prev] * s * s + Ds[j] * c * c;
           Ds[prev] = tt;
           flag[prev] = 1;
@@ -187,7 +208,8 @@ __global__ void dc_deflate_kernel(const Merge *merges, const double *e, DcWork W
 }
 
 // K3: apply the recorded rotations to the Q columns (each thread owns a row of the block).
-__global__ void dc_rotate_kernel(const Merge *merges, double *Q, int ldq, DcWork W) {
+template <typename T>
+__global__ void dc_rotate_kernel(const Merge *merges, T *Q, int ldq, DcWork<T> W) {
   const int mi = blockIdx.x;
   Merge mg = merges[mi];
   if (mg.m == mg.b) return;
@@ -197,16 +219,17 @@ __global__ void dc_rotate_kernel(const Merge *merges, double *Q, int ldq, DcWork
   if (row >= mg.b) return;
   for (int k = 0; k < nrot; ++k) {
     int cp = W.rot_cols[2 * (mg.a + k)], cj = W.rot_cols[2 * (mg.a + k) + 1];
-    double c = W.rot_cs[2 * (mg.a + k)], s = W.rot_cs[2 * (mg.a + k) + 1];
-    double x = Q[row + (size_t)cp * ldq], y = Q[row + (size_t)cj * ldq];
+    T c = W.rot_cs[2 * (mg.a + k)], s = W.rot_cs[2 * (mg.a + k) + 1];
+    T x = Q[row + (size_t)cp * ldq], y = Q[row + (size_t)cj * ldq];
     Q[row + (size_t)cp * ldq] = c * x + s * y;
     Q[row + (size_t)cj * ldq] = c * y - s * x;
   }
 }
 
 // K4: secular equation, one warp per root.
-__global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_merge, const double *e,
-                                  DcWork W, int *status) {
+template <typename T>
+__global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_merge, const T *e,
+                                  DcWork<T> W, int *status) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= n) return;
@@ -217,75 +240,75 @@ __global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_mer
   const int K = W.mK[mi];
   const int i = g - a;
   if (i >= K) return;
-  const double rho = 2.0 * fabs(e[mg.m - 1]);
-  const double *dl = W.dl + a, *w = W.w + a;
+  const T rho = T(2) * fabs(e[mg.m - 1]);
+  const T *dl = W.dl + a, *w = W.w + a;
   int org;
-  double lo, hi, tau;
+  T lo, hi, tau;
   if (i < K - 1) {
-    double mid = 0.5 * (dl[i + 1] - dl[i]);
-    double s = 0.0;
+    T mid = T(0.5) * (dl[i + 1] - dl[i]);
+    T s = T(0);
     for (int j = lane; j < K; j += 32) s += w[j] * w[j] / ((dl[j] - dl[i]) - mid);
-    double f = 1.0 + rho * wsum(s);
-    if (f > 0.0) { org = i; lo = 0.0; hi = mid; }
-    else { org = i + 1; lo = -mid; hi = 0.0; }
+    T f = T(1) + rho * wsum(s);
+    if (f > T(0)) { org = i; lo = T(0); hi = mid; }
+    else { org = i + 1; lo = -mid; hi = T(0); }
   } else {
-    double s = 0.0;
+    T s = T(0);
     for (int j = lane; j < K; j += 32) s += w[j] * w[j];
     org = K - 1;
-    lo = 0.0;
+    lo = T(0);
     hi = rho * wsum(s);
   }
-  tau = 0.5 * (lo + hi);
-  const double dorg = dl[org];
+  tau = T(0.5) * (lo + hi);
+  const T dorg = dl[org];
   bool conv = false;
   for (int it = 0; it < kSecularMaxIter; ++it) {
-    double sf = 0.0, sp = 0.0, sq = 0.0, sa = 0.0;
+    T sf = T(0), sp = T(0), sq = T(0), sa = T(0);
     for (int j = lane; j < K; j += 32) {
-      double dd = (dl[j] - dorg) - tau;
-      double t = w[j] * w[j] / dd;
+      T dd = (dl[j] - dorg) - tau;
+      T t = w[j] * w[j] / dd;
       sf += t;
       sa += fabs(t);
       if (j <= i) sp += t / dd; else sq += t / dd;
     }
-    double f = 1.0 + rho * wsum(sf);
-    double psip = rho * wsum(sp);
-    double phip = rho * wsum(sq);
+    T f = T(1) + rho * wsum(sf);
+    T psip = rho * wsum(sp);
+    T phip = rho * wsum(sq);
     // rounding-error bound of the evaluated f (cf. the ERRETM test of LAPACK's dlaed4)
-    double ferr = kEps * (8.0 * (1.0 + rho * wsum(sa)) + fabs(tau) * (psip + phip));
-    if (f > 0.0) hi = tau; else lo = tau;
+    T ferr = Lim<T>::eps * (T(8) * (T(1) + rho * wsum(sa)) + fabs(tau) * (psip + phip));
+    if (f > T(0)) hi = tau; else lo = tau;
     if (fabs(f) <= ferr) { conv = true; break; }
-    double nt;
+    T nt;
     if (i < K - 1) {
-      double dlo = (dl[i] - dorg) - tau, dhi = (dl[i + 1] - dorg) - tau;
-      double A = psip * dlo * dlo, B = phip * dhi * dhi;
-      double c = f - A / dlo - B / dhi;
-      double A2 = c, B2 = -(c * (dlo + dhi) + A + B), C2 = c * dlo * dhi + A * dhi + B * dlo;
-      double st;
-      if (A2 == 0.0) {
-        st = (B2 != 0.0) ? -C2 / B2 : 0.0;
+      T dlo = (dl[i] - dorg) - tau, dhi = (dl[i + 1] - dorg) - tau;
+      T A = psip * dlo * dlo, B = phip * dhi * dhi;
+      T c = f - A / dlo - B / dhi;
+      T A2 = c, B2 = -(c * (dlo + dhi) + A + B), C2 = c * dlo * dhi + A * dhi + B * dlo;
+      T st;
+      if (A2 == T(0)) {
+        st = (B2 != T(0)) ? -C2 / B2 : 0.0;
       } else {
-        double disc = sqrt(fmax(B2 * B2 - 4.0 * A2 * C2, 0.0));
-        double s1, s2;
-        if (B2 <= 0.0) {
-          double den = -B2 + disc;
-          s1 = den / (2.0 * A2);
-          s2 = (den != 0.0) ? 2.0 * C2 / den : s1;
+        T disc = sqrt(fmax(B2 * B2 - T(4) * A2 * C2, T(0)));
+        T s1, s2;
+        if (B2 <= T(0)) {
+          T den = -B2 + disc;
+          s1 = den / (T(2) * A2);
+          s2 = (den != T(0)) ? T(2) * C2 / den : s1;
         } else {
-          double den = -B2 - disc;
-          s1 = den / (2.0 * A2);
-          s2 = 2.0 * C2 / den;
+          T den = -B2 - disc;
+          s1 = den / (T(2) * A2);
+          s2 = T(2) * C2 / den;
         }
         st = (s2 > dlo && s2 < dhi) ? s2 : s1;
       }
       nt = tau + st;
     } else {
-      double dlo = (dl[K - 1] - dorg) - tau;
-      double A = psip * dlo * dlo;
-      double c = f - A / dlo;
-      nt = tau + ((c != 0.0) ? dlo + A / c : 0.0);
+      T dlo = (dl[K - 1] - dorg) - tau;
+      T A = psip * dlo * dlo;
+      T c = f - A / dlo;
+      nt = tau + ((c != T(0)) ? dlo + A / c : 0.0);
     }
-    if (!(nt > lo && nt < hi)) nt = 0.5 * (lo + hi);
-    if (nt == tau || fabs(hi - lo) <= 2.0 * kEps * fmax(fabs(lo), fabs(hi))) {
+    if (!(nt > lo && nt < hi)) nt = T(0.5) * (lo + hi);
+    if (nt == tau || fabs(hi - lo) <= T(2) * Lim<T>::eps * fmax(fabs(lo), fabs(hi))) {
       tau = nt;
       conv = true;
       break;
@@ -301,7 +324,8 @@ __global__ void dc_secular_kernel(int n, const Merge *merges, const int *pos_mer
 }
 
 // K5: Gu-Eisenstat zhat, one warp per j; product of O(1) ratios with exponent tracking.
-__global__ void dc_zhat_kernel(int n, const Merge *merges, const int *pos_merge, const double *e, DcWork W) {
+template <typename T>
+__global__ void dc_zhat_kernel(int n, const Merge *merges, const int *pos_merge, const T *e, DcWork<T> W) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= n) return;
@@ -312,41 +336,42 @@ __global__ void dc_zhat_kernel(int n, const Merge *merges, const int *pos_merge,
   const int K = W.mK[mi];
   const int j = g - a;
   if (j >= K) return;
-  const double rho = 2.0 * fabs(e[mg.m - 1]);
-  const double *dl = W.dl + a;
-  const double dj = dl[j];
-  double p = 1.0;
+  const T rho = T(2) * fabs(e[mg.m - 1]);
+  const T *dl = W.dl + a;
+  const T dj = dl[j];
+  T p = 1.0;
   int ex = 0;
   for (int i = lane; i < K; i += 32) {
-    double num = (dl[W.org[a + i]] - dj) + W.tau[a + i];
-    double r = (i == j) ? num / rho : num / (dl[i] - dj);
+    T num = (dl[W.org[a + i]] - dj) + W.tau[a + i];
+    T r = (i == j) ? num / rho : num / (dl[i] - dj);
     p *= r;
-    double ap = fabs(p);
-    if (ap > 1e150 || (ap < 1e-150 && ap > 0.0)) {
+    T ap = fabs(p);
+    if (ap > Lim<T>::big || (ap < Lim<T>::small && ap > T(0))) {
       int k;
-      p = frexp(p, &k);
+      p = t_frexp(p, &k);
       ex += k;
     }
   }
   // combine lane products
   for (int o = 16; o > 0; o >>= 1) {
-    double po = __shfl_xor_sync(0xffffffffu, p, o);
+    T po = __shfl_xor_sync(0xffffffffu, p, o);
     int eo = __shfl_xor_sync(0xffffffffu, ex, o);
     p *= po;
     ex += eo;
     int k;
-    p = frexp(p, &k);
+    p = t_frexp(p, &k);
     ex += k;
   }
   if (lane == 0) {
-    double val = ldexp(p, ex);
-    double z = sqrt(fmax(val, 0.0));
+    T val = t_ldexp(p, ex);
+    T z = sqrt(fmax(val, T(0)));
     W.zh[a + j] = copysign(z, W.w[a + j]);
   }
 }
 
 // K6: eigenvector matrix of the rank-one problem, one warp per column i; U rows [0,K) at column a+i.
-__global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_merge, DcWork W, int ldu) {
+template <typename T>
+__global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_merge, DcWork<T> W, int ldu) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= n) return;
@@ -357,23 +382,24 @@ __global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_mer
   const int K = W.mK[mi];
   const int i = g - a;
   if (i >= K) return;
-  const double *dl = W.dl + a;
-  const double dorg = dl[W.org[a + i]];
-  const double tau = W.tau[a + i];
-  double *u = W.U + (size_t)(a + i) * ldu;
-  double s = 0.0;
+  const T *dl = W.dl + a;
+  const T dorg = dl[W.org[a + i]];
+  const T tau = W.tau[a + i];
+  T *u = W.U + (size_t)(a + i) * ldu;
+  T s = T(0);
   for (int t = lane; t < K; t += 32) {
-    double v = W.zh[a + t] / ((dl[t] - dorg) - tau);
+    T v = W.zh[a + t] / ((dl[t] - dorg) - tau);
     u[t] = v;
     s += v * v;
   }
-  double inv = 1.0 / sqrt(wsum(s));
+  T inv = T(1) / sqrt(wsum(s));
   for (int t = lane; t < K; t += 32) u[t] *= inv;
 }
 
 // K7: gather the non-deflated Q columns (rows [a,b)) into Gs at columns a .. a+K-1.
-__global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merge, const double *Q, int ldq,
-                                 DcWork W, int ldg) {
+template <typename T>
+__global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merge, const T *Q, int ldq,
+                                 DcWork<T> W, int ldg) {
   const int g = blockIdx.x;
   const int mi = pos_merge[g];
   if (mi < 0) return;
@@ -388,23 +414,25 @@ __global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merg
 }
 
 // K8 (small merges): Qtmp[a:b, a:a+K] = Gs[a:b, a:a+K] * U[0:K, a:a+K] inside one CTA.
-__global__ void dc_small_gemm_kernel(const Merge *merges, DcWork W, int ld) {
+template <typename T>
+__global__ void dc_small_gemm_kernel(const Merge *merges, DcWork<T> W, int ld) {
   Merge mg = merges[blockIdx.x];
   if (mg.m == mg.b) return;
   const int K = W.mK[blockIdx.x];
   const int a = mg.a, N = mg.b - mg.a;
   for (int idx = threadIdx.x; idx < N * K; idx += blockDim.x) {
     int r = idx % N, c = idx / N;
-    double s = 0.0;
-    const double *g = W.Gs + (a + r) + (size_t)a * ld;
-    const double *u = W.U + (size_t)(a + c) * ld;
+    T s = T(0);
+    const T *g = W.Gs + (a + r) + (size_t)a * ld;
+    const T *u = W.U + (size_t)(a + c) * ld;
     for (int t = 0; t < K; ++t) s = fma(g[(size_t)t * ld], u[t], s);
     W.Qtmp[(a + r) + (size_t)(a + c) * ld] = s;
   }
 }
 
 // K9: final ascending order (rank in the union of roots and deflated values, ties by index).
-__global__ void dc_rank_kernel(const Merge *merges, double *d, DcWork W) {
+template <typename T>
+__global__ void dc_rank_kernel(const Merge *merges, T *d, DcWork<T> W) {
   const int mi = blockIdx.x;
   Merge mg = merges[mi];
   const int a = mg.a, N = mg.b - mg.a;
@@ -416,13 +444,13 @@ __global__ void dc_rank_kernel(const Merge *merges, double *d, DcWork W) {
     return;
   }
   const int K = W.mK[mi];
-  auto value = [&](int k) -> double {
+  auto value = [&](int k) -> T {
     return (k < K) ? W.lam[a + k] : W.Ds[a + W.dfpos[a + (k - K)]];
   };
-  double v = value(e0);
+  T v = value(e0);
   int rank = 0;
   for (int k = 0; k < N; ++k) {
-    double u = value(k);
+    T u = value(k);
     if (u < v || (u == v && k < e0)) ++rank;
   }
   W.vals[a + rank] = v;
@@ -431,13 +459,14 @@ __global__ void dc_rank_kernel(const Merge *merges, double *d, DcWork W) {
 }
 
 // K10: scatter the columns into the output buffer and the values into d.
-__global__ void dc_scatter_kernel(int n, const int *pos_merge_all, const Merge *merges, const double *Q,
-                                  int ldq, double *Qout, double *d, DcWork W, int ldt) {
+template <typename T>
+__global__ void dc_scatter_kernel(int n, const int *pos_merge_all, const Merge *merges, const T *Q,
+                                  int ldq, T *Qout, T *d, DcWork<T> W, int ldt) {
   const int g = blockIdx.x;
   const int mi = pos_merge_all[g];
   Merge mg = merges[mi];
   int src = W.srcinfo[g];
-  const double *col = (src >= 0) ? Q + (size_t)src * ldq : W.Qtmp + (size_t)(-src - 1) * ldt;
+  const T *col = (src >= 0) ? Q + (size_t)src * ldq : W.Qtmp + (size_t)(-src - 1) * ldt;
   for (int r = mg.a + threadIdx.x; r < mg.b; r += blockDim.x) Qout[r + (size_t)g * ldq] = col[r];
   if (threadIdx.x == 0) d[g] = W.vals[g];
 }
@@ -494,19 +523,19 @@ size_t stedc_iwork_size(int n) {
   return (size_t)n * (10 + 1 + 4 + 2 * (size_t)(levels + 1)) + 64;
 }
 
-int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, double *work, int *iwork,
-          int *status_dev) {
+template <typename T>
+int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork, int *status_dev) {
   if (n <= 0) return 0;
   if (ldq != n) return -1;  // the workspace layout assumes a square, tightly packed Q
   dim3 gi(ceil_div(n, 256), n);
-  dc_identity_kernel<<<gi, 256, 0, s>>>(n, Q, ldq);
+  dc_identity_kernel<T><<<gi, 256, 0, s>>>(n, Q, ldq);
   count_launch();
   if (n == 1) return 0;
   std::vector<int> bounds;
   std::vector<DcLevel> levels = plan_levels(n, bounds);
 
-  DcWork W;
-  double *p = work;
+  DcWork<T> W;
+  T *p = work;
   W.Ds = p; p += n; W.zs = p; p += n; W.dl = p; p += n; W.w = p; p += n; W.tau = p; p += n;
   W.lam = p; p += n; W.zh = p; p += n; W.vals = p; p += n; p += n;
   W.rot_cs = p; p += 2 * (size_t)n;
@@ -532,13 +561,13 @@ int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, doubl
   // the metadata lives in a dedicated device allocation owned by the caller's iwork tail
   cudaMemcpyAsync(dev_meta, meta.data(), meta.size() * sizeof(int), cudaMemcpyHostToDevice, s);
 
-  dc_tear_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
+  dc_tear_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
   count_launch();
   // The merge at level L reads whole blocks [a,b)^2 whose off-diagonal sub-blocks must be zero;
   // the scatter only writes inside the current blocks, so the second buffer starts zeroed.
-  cudaMemsetAsync(W.Qalt, 0, sizeof(double) * (size_t)n * n, s);
+  cudaMemsetAsync(W.Qalt, 0, sizeof(T) * (size_t)n * n, s);
 
-  double *Qin = Q, *Qout = W.Qalt;
+  T *Qin = Q, *Qout = W.Qalt;
   std::vector<int> hK;
   for (size_t li = 0; li < levels.size(); ++li) {
     DcLevel &L = levels[li];
@@ -546,18 +575,18 @@ int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, doubl
     const int *pm = dev_meta + off_pm[li];
     const int *pma = dev_meta + off_pma[li];
     int nm = (int)L.merges.size();
-    dc_sort_kernel<<<nm, 256, 0, s>>>(dm, d, e, Qin, ldq, W);
-    dc_deflate_kernel<<<nm, 256, 0, s>>>(dm, e, W);
+    dc_sort_kernel<T><<<nm, 256, 0, s>>>(dm, d, e, Qin, ldq, W);
+    dc_deflate_kernel<T><<<nm, 256, 0, s>>>(dm, e, W);
     dim3 gr(nm, ceil_div(L.max_block, 256));
-    dc_rotate_kernel<<<gr, 256, 0, s>>>(dm, Qin, ldq, W);
+    dc_rotate_kernel<T><<<gr, 256, 0, s>>>(dm, Qin, ldq, W);
     int warps_blocks = ceil_div((long long)n * 32, 256);
-    dc_secular_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W, status_dev);
-    dc_zhat_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W);
-    dc_build_u_kernel<<<warps_blocks, 256, 0, s>>>(n, dm, pm, W, n);
-    dc_gather_kernel<<<n, 128, 0, s>>>(n, dm, pm, Qin, ldq, W, n);
+    dc_secular_kernel<T><<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W, status_dev);
+    dc_zhat_kernel<T><<<warps_blocks, 256, 0, s>>>(n, dm, pm, e, W);
+    dc_build_u_kernel<T><<<warps_blocks, 256, 0, s>>>(n, dm, pm, W, n);
+    dc_gather_kernel<T><<<n, 128, 0, s>>>(n, dm, pm, Qin, ldq, W, n);
     count_launch(7);
     if (L.max_block <= kSmallMerge) {
-      dc_small_gemm_kernel<<<nm, 256, 0, s>>>(dm, W, n);
+      dc_small_gemm_kernel<T><<<nm, 256, 0, s>>>(dm, W, n);
       count_launch();
     } else {
       hK.resize(nm);
@@ -567,21 +596,24 @@ int stedc(cudaStream_t s, int n, double *d, double *e, double *Q, int ldq, doubl
         const Merge &mg = L.merges[k];
         if (mg.m == mg.b || hK[k] == 0) continue;
         int a = mg.a, N = mg.b - mg.a, K = hK[k];
-        dgemm(s, 'N', 'N', N, K, K, 1.0, W.Gs + a + (size_t)a * n, n, W.U + (size_t)a * n, n, 0.0,
-              W.Qtmp + a + (size_t)a * n, n);
+        gemm<T>(s, 'N', 'N', N, K, K, T(1), W.Gs + a + (size_t)a * n, n, W.U + (size_t)a * n, n, T(0),
+                W.Qtmp + a + (size_t)a * n, n);
       }
     }
     dim3 grk(nm, ceil_div(L.max_block, 256));
-    dc_rank_kernel<<<grk, 256, 0, s>>>(dm, d, W);
-    dc_scatter_kernel<<<n, 128, 0, s>>>(n, pma, dm, Qin, ldq, Qout, d, W, n);
+    dc_rank_kernel<T><<<grk, 256, 0, s>>>(dm, d, W);
+    dc_scatter_kernel<T><<<n, 128, 0, s>>>(n, pma, dm, Qin, ldq, Qout, d, W, n);
     count_launch(2);
     std::swap(Qin, Qout);
   }
   if (Qin != Q) {
-    cudaMemcpyAsync(Q, Qin, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(Q, Qin, sizeof(T) * (size_t)n * n, cudaMemcpyDeviceToDevice, s);
   }
   return 0;
 }
+
+template int stedc<double>(cudaStream_t, int, double *, double *, double *, int, double *, int *, int *);
+template int stedc<float>(cudaStream_t, int, float *, float *, float *, int, float *, int *, int *);
 
 // ------------------------------------------------------------------------------------- no-alloc
 // Allocation-free variant for callers that cannot allocate device memory (a solver step running
@@ -629,7 +661,7 @@ __global__ void dc_plan_kernel(int n, DcPlanOffsets P, int *meta) {
 
 static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_in, double *Q, double *scratch) {
   double *e = const_cast<double *>(e_in);  // read only
-  DcWork W;
+  DcWork<double> W;
   double *p = scratch;
   W.Ds = p; p += n; W.zs = p; p += n; W.dl = p; p += n; W.w = p; p += n; W.tau = p; p += n;
   W.lam = p; p += n; W.zh = p; p += n; W.vals = p; p += n; p += n;
@@ -656,11 +688,11 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
   }
   cudaMemsetAsync(status, 0, sizeof(int), s);
   dim3 gi(ceil_div(n, 256), n);
-  dc_identity_kernel<<<gi, 256, 0, s>>>(n, Q, n);
+  dc_identity_kernel<double><<<gi, 256, 0, s>>>(n, Q, n);
   count_launch();
   if (n == 1) return 0;
   dc_plan_kernel<<<1, 256, 0, s>>>(n, P, meta);
-  dc_tear_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
+  dc_tear_kernel<double><<<ceil_div(n, 256), 256, 0, s>>>(n, d, e);
   count_launch(2);
   cudaMemsetAsync(W.Qalt, 0, sizeof(double) * (size_t)n * n, s);
   double *Qin = Q, *Qout = W.Qalt;
@@ -670,18 +702,18 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
     const int *pma = meta + P.off_pma[L];
     const int nm = P.nm[L];
     const int max_block = std::min(1 << L, n);
-    dc_sort_kernel<<<nm, 256, 0, s>>>(dm, d, e, Qin, n, W);
-    dc_deflate_kernel<<<nm, 256, 0, s>>>(dm, e, W);
+    dc_sort_kernel<double><<<nm, 256, 0, s>>>(dm, d, e, Qin, n, W);
+    dc_deflate_kernel<double><<<nm, 256, 0, s>>>(dm, e, W);
     dim3 gr(nm, ceil_div(max_block, 256));
-    dc_rotate_kernel<<<gr, 256, 0, s>>>(dm, Qin, n, W);
+    dc_rotate_kernel<double><<<gr, 256, 0, s>>>(dm, Qin, n, W);
     int wb = ceil_div((long long)n * 32, 256);
-    dc_secular_kernel<<<wb, 256, 0, s>>>(n, dm, pm, e, W, status);
-    dc_zhat_kernel<<<wb, 256, 0, s>>>(n, dm, pm, e, W);
-    dc_build_u_kernel<<<wb, 256, 0, s>>>(n, dm, pm, W, n);
-    dc_gather_kernel<<<n, 128, 0, s>>>(n, dm, pm, Qin, n, W, n);
+    dc_secular_kernel<double><<<wb, 256, 0, s>>>(n, dm, pm, e, W, status);
+    dc_zhat_kernel<double><<<wb, 256, 0, s>>>(n, dm, pm, e, W);
+    dc_build_u_kernel<double><<<wb, 256, 0, s>>>(n, dm, pm, W, n);
+    dc_gather_kernel<double><<<n, 128, 0, s>>>(n, dm, pm, Qin, n, W, n);
     count_launch(7);
     if (max_block <= kSmallMerge) {
-      dc_small_gemm_kernel<<<nm, 256, 0, s>>>(dm, W, n);
+      dc_small_gemm_kernel<double><<<nm, 256, 0, s>>>(dm, W, n);
       count_launch();
     } else {
       // at most two merges at this size (n <= 256): read their sizes into a stack buffer
@@ -696,8 +728,8 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
       }
     }
     dim3 grk(nm, ceil_div(max_block, 256));
-    dc_rank_kernel<<<grk, 256, 0, s>>>(dm, d, W);
-    dc_scatter_kernel<<<n, 128, 0, s>>>(n, pma, dm, Qin, n, Qout, d, W, n);
+    dc_rank_kernel<double><<<grk, 256, 0, s>>>(dm, d, W);
+    dc_scatter_kernel<double><<<n, 128, 0, s>>>(n, pma, dm, Qin, n, Qout, d, W, n);
     count_launch(2);
     std::swap(Qin, Qout);
   }

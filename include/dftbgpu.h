@@ -32,7 +32,10 @@ enum {
 /* Precision forms of the SCC cycle. */
 enum {
   DFTBGPU_PREC_FP64 = 0,   /* plain FP64 drop-in */
-  DFTBGPU_PREC_MIXED = 1   /* reduced-precision early iterations, FP64-refined final iteration */
+  DFTBGPU_PREC_MIXED = 1   /* FP32 eigensolves (transform, tridiagonalisation, divide and conquer,
+                              back-transformation, density matrix) for the early SCC iterations;
+                              Cholesky, Fermi filling, Mulliken, energies and mixing stay FP64;
+                              the cycle finishes and converges in FP64 */
 };
 
 typedef struct dftbgpu_ctx dftbgpu_ctx;
@@ -51,6 +54,8 @@ typedef struct {
   double net_charge;      /* Charge (e); N_el = sum(reference occupations) - net_charge */
   int precision;          /* DFTBGPU_PREC_* */
   int convergent_only;    /* ConvergentSCCOnly: return DFTBGPU_ERR_SCC_NOT_CONVERGED if 1 */
+  double mixed_switch_tol;/* mixed form: leave reduced precision once max|q_out - q_in| < this
+                             (0 = default 1e-4); the converged iteration is always FP64 */
 } dftbgpu_scc_opts;
 
 /* Energy terms as in dftb/energytypes.F90 (TEnergies) for this path. */
@@ -109,6 +114,18 @@ int dftbgpu_scc(dftbgpu_ctx *ctx, const dftbgpu_scc_opts *opts, const double *q_
                 double *q_out, int *n_iter, int *converged);
 
 /*
+ * Per-iteration record of the last dftbgpu_scc call, the data of the SCC iteration table the
+ * reference prints (dftbplus/mainio.F90:4781-4845, printSccHeader/printSccInfo: iSCC, total
+ * electronic energy, its change, SCC error): energy[i] = Eelec = EnonSCC + Escc of iteration i
+ * (from its output charges), error[i] = max|q_out - q_in|,
+ * precision[i] = DFTBGPU_PREC_FP64 or DFTBGPU_PREC_MIXED (an FP32 eigensolve), ms[i] = host wall
+ * time of the iteration. Writes min(cap, count) entries (each array may be NULL) and returns the
+ * iteration count, or -1 for a NULL context or cap < 0.
+ */
+int dftbgpu_scc_history(const dftbgpu_ctx *ctx, int cap, double *energy, double *error, int *precision,
+                        double *ms);
+
+/*
  * Energy gradient (not forces) of the converged state, grad[3*natom] (x,y,z per atom).
  * Energy-weighted density matrix + derivative_blockEuclidean (dftb/forces.F90:548-669, FD SK
  * derivatives nonscc.F90:428-484) + SCC double-counting (scc.F90:794-843) + repulsive
@@ -143,9 +160,9 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  *   0 H0/S build + Cholesky, 1 potentials + H assembly, 2 L^-1 H L^-T, 3 tridiagonalisation,
  *   4 tridiagonal divide and conquer, 5 Fermi filling, 6 back-transformation (Q Z, L^-T Y),
  *   7 density matrix, 8 Mulliken + energies, 9 Broyden mixing, 10 gradients, 11 FP64 GEMM (all
- *   GEMM launches, overlapping the phases above).
- * enable: 1 resets and starts accumulating, 0 stops. read: ms[12], flops[12] (algorithmic FLOPs
- * per phase as counted for the roofline), calls[12]; returns the number of phases written.
+ *   FP64 GEMM launches, overlapping the phases above), 12 FP32 GEMM (mixed form, likewise).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[13], flops[13] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[13]; returns the number of phases written.
  */
 int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);

@@ -150,6 +150,32 @@ def test_spd_scc(gpu_lib, tio2_model):
     _scc_parity(tio2_model, c, s, kT=5e-3)
 
 
+@pytest.mark.parametrize("n_mol,radius,seed", [(32, 10.0, 1), (128, 20.0, 128)])
+def test_mixed_precision_matches_fp64(gpu_lib, water_model, n_mol, radius, seed):
+    """Mixed form: FP32 eigensolves early, FP64 to convergence. Errors against the FP64 oracle must
+    meet the mixed targets (|dE| <= 1e-6 Ha/atom, max|dF| <= 1e-5 Ha/Bohr); in practice they are at
+    the SCC-tolerance level."""
+    from dftbplus_gb300 import binding, synth
+    c, s = synth.water_cluster(n_mol, radius, seed)
+    sys_ = O.System(water_model, c, s)
+    ref = O.run_scc(sys_, kt=1e-3, scc_tol=1e-7)
+    ctx = _ctx(water_model, c, s)
+    ctx.profile(True)
+    res = ctx.scc(binding.default_opts(kT=1e-3, scc_tol=1e-7, precision=binding.PREC_MIXED))
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    assert res["converged"]
+    assert prof["gemm_fp32"]["calls"] > 0, "no reduced-precision iteration ran"
+    natom = len(s)
+    de = abs(res["energies"]["EMermin"] - ref.energies["EMermin"])
+    assert de / natom < 1e-8
+    assert np.max(np.abs(res["q_out"] - ref.q_out_atom)) < 1e-6
+    g = ctx.gradients()
+    gref = O.gradients(sys_, ref)
+    assert np.max(np.abs(g - gref)) < 1e-6
+    ctx.close()
+
+
 def test_not_positive_definite_reports_status(gpu_lib):
     """A table draw with an indefinite overlap: the Cholesky reports the status, no fault."""
     from dftbplus_gb300 import binding, synth
