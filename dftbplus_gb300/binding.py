@@ -24,6 +24,7 @@ _ip = C.POINTER(C.c_int)
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+ITER_PERTURB = 2   # scc_history: perturbative update around the last FP64 iteration
 
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "overlap not positive definite",
           4: "SCC not converged", 5: "Fermi level search failed", 6: "iteration cap reached",
@@ -72,7 +73,7 @@ SIGNATURES = {
 }
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
-          "density", "mulliken_energy", "broyden", "gradients", "gemm_fp64", "gemm_fp32"]
+          "density", "mulliken_energy", "broyden", "gradients", "perturbation", "gemm_fp64", "gemm_fp32"]
 
 _lib = None
 

@@ -55,6 +55,12 @@ struct Ctx {
         *wk32_ormtr = nullptr, *wk32_stedc = nullptr;
   bool mixed_ready = false;
   int mixed_iters = 0;    // FP32 iterations of the last SCC call
+  // perturbative iterations of the mixed form: reference density and potentials of the last FP64
+  // iteration, M^T / response matrix and C dP (n x n FP32); the FP32 LOW-iteration buffers hold
+  // C (C32), X = S C (V32), diag(dV) C (T32), diag(dV) X (Z32) and drho (A32) meanwhile
+  size_t cap_pert = 0, cap_pert_atoms = 0;
+  float *Mt32 = nullptr, *Zp32 = nullptr;
+  double *rho_ref = nullptr, *Vref = nullptr;
   // per-iteration record of the last SCC call: electronic energy, max|q_out - q_in|, precision, host ms
   std::vector<double> hist_e, hist_err, hist_ms;
   std::vector<int> hist_prec;
@@ -291,6 +297,21 @@ static int ensure_mixed(Ctx *c, int n) {
   return DFTBGPU_OK;
 }
 
+static int ensure_pert(Ctx *c, int n, int natom) {
+  if ((size_t)n > c->cap_pert) {
+    size_t nn = (size_t)n * n;
+    DG_CHECK(c, dev_alloc(c, &c->Mt32, nn));
+    DG_CHECK(c, dev_alloc(c, &c->Zp32, nn));
+    DG_CHECK(c, dev_alloc(c, &c->rho_ref, nn));
+    c->cap_pert = n;
+  }
+  if ((size_t)natom > c->cap_pert_atoms) {
+    DG_CHECK(c, dev_alloc(c, &c->Vref, (size_t)natom));
+    c->cap_pert_atoms = natom;
+  }
+  return DFTBGPU_OK;
+}
+
 static ModelDev model_view(Ctx *c) { return ModelDev{c->nsp, c->d_sp, c->d_pair, c->d_tab, c->d_rep}; }
 static GeomDev geom_view(Ctx *c) { return GeomDev{c->natom, c->norb, c->d_xyz, c->d_species, c->d_orb}; }
 
@@ -307,8 +328,9 @@ static int check_status(Ctx *c, const char *stage) {
 // Generalized eigensolve of H (full symmetric, destroyed) with the stored L^-1. Eigenvalues into
 // c->eig; the eigenvectors of the first k levels into c->C (columns), k chosen by pick_k after the
 // eigenvalues are known (the Fermi filling decides how many levels the density matrix needs).
+// all_vectors: back-transform all n eigenvectors (c->Z = Y, c->C = L^-T Y), k is still returned.
 template <class PickK>
-static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = false) {
+static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = false, bool all_vectors = false) {
   cudaStream_t s = c->stream;
   const double nd = (double)n;
   if (!reduced) {
@@ -320,7 +342,7 @@ static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = fa
   }
   mark(c, kPhSytrd);
   prof_flops(c, kPhSytrd, 4.0 / 3.0 * nd * nd * nd);
-  sytrd_lower(s, n, Hm, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
+  sytrd_lower(s, n, Hm, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd, c->d_status);
   mark(c, kPhStedc);
   int rc = stedc(s, n, c->dd, c->ee, c->Z, n, c->wk_stedc, c->iwk_stedc, c->d_status);
   if (rc != 0) return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
@@ -329,10 +351,11 @@ static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = fa
   int k = 0;
   DG_CHECK(c, pick_k(&k));
   mark(c, kPhBack);
-  if (k > 0) {
-    prof_flops(c, kPhBack, 3.0 * nd * nd * (double)k);
-    ormtr_left(s, n, k, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
-    dgemm(s, 'T', 'N', n, k, n, 1.0, c->Linv, n, c->Z, n, 0.0, c->C, n, kAUpper);
+  const int kb = all_vectors ? n : k;
+  if (kb > 0) {
+    prof_flops(c, kPhBack, 3.0 * nd * nd * (double)kb);
+    ormtr_left(s, n, kb, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
+    dgemm(s, 'T', 'N', n, kb, n, 1.0, c->Linv, n, c->Z, n, 0.0, c->C, n, kAUpper);
   }
   return DFTBGPU_OK;
 }
@@ -406,7 +429,7 @@ int dftbgpu_destroy(dftbgpu_ctx *c) {
                   c->wk_ormtr, c->wk_stedc, c->iwk_stedc, c->d_status, c->d_scal, c->bro.ww, c->bro.aa,
                   c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast, c->L32, c->Li32, c->A0_32, c->A32,
                   c->T32, c->V32, c->Z32, c->C32, c->d32, c->e32, c->tau32, c->wk32_sytrd, c->wk32_ormtr,
-                  c->wk32_stedc};
+                  c->wk32_stedc, c->Mt32, c->Zp32, c->rho_ref, c->Vref};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   cudaStreamDestroy(c->stream);
@@ -621,11 +644,24 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   double h_scal[kSCount];
   int it = 0;
   bool conv = false;
-  // Mixed form: reduced-precision (FP32) eigensolves until max|q_out - q_in| < switch_tol, then FP64
-  // to convergence (the converged state is always an FP64 iteration).
-  bool low = (o->precision == DFTBGPU_PREC_MIXED);
-  const double switch_tol = (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 1e-4;
-  if (low) DG_CHECK(c, ensure_mixed(c, n));
+  // Mixed form, three kinds of iteration:
+  //   LOW  FP32 eigensolve (transform, tridiagonalisation, divide and conquer, back-transform,
+  //        density) until max|q_out - q_in| < switch_tol;
+  //   FULL FP64 eigensolve with all eigenvectors, which becomes the reference of
+  //   PERT first-order density-matrix perturbation around the last FULL iteration (FP32 GEMMs on
+  //        the potential change only), until converged; then FULL again at the same charges.
+  // The cycle only ends on a converged FULL iteration, so every returned state is FP64. The plain
+  // form runs FULL iterations (with k eigenvectors) throughout.
+  enum { kFormLow, kFormFull, kFormPert };
+  const bool mixed = (o->precision == DFTBGPU_PREC_MIXED);
+  int form = mixed ? kFormLow : kFormFull;
+  const double switch_tol = (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 1e-3;
+  constexpr int kMaxPertRun = 16;   // perturbative iterations before the reference is renewed
+  int pert_run = 0, k_ref = 0;
+  if (mixed) {
+    DG_CHECK(c, ensure_mixed(c, n));
+    DG_CHECK(c, ensure_pert(c, n, N));
+  }
   c->mixed_iters = 0;
   c->hist_e.clear(); c->hist_err.clear(); c->hist_ms.clear(); c->hist_prec.clear();
   int mix_calls = 0;
@@ -635,25 +671,41 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     DG_CUDA(c, cudaStreamSynchronize(s));
     int st = 0;
     DG_CUDA(c, cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-    if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "eigensolver: secular iteration cap reached");
+    if (st == kDevIterCap) return set_error(c, DFTBGPU_ERR_ITER_CAP, "eigensolver: a bounded device loop hit its cap (secular iteration or grid barrier)");
     if (h_scal[kSFermiStatus] != 0.0) return set_error(c, DFTBGPU_ERR_FERMI, "Fermi level search did not converge.");
     *kout = (int)h_scal[kSNLevels];
     return DFTBGPU_OK;
   };
   for (it = 1; it <= o->max_iter; ++it) {
     const auto t_it = std::chrono::steady_clock::now();
-    const bool it_low = low;
+    if (mixed && it == o->max_iter) form = kFormFull;   // the last allowed iteration is FP64
+    const int it_form = form;
     mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
     int k = 0;
-    if (low) {
+    if (form == kFormPert) {
+      // rho = rho_ref + C dP C^T with dP from M = C^T dH C, dH = 1/2 (S D + D S), D = diag(V - Vref)
+      mark(c, kPhPert);
+      const double nd = (double)n;
+      k = k_ref;
+      prof_flops(c, kPhPert, 8.0 * nd * nd * (double)k);
+      dmpt_scale(s, g, c->d_V, c->Vref, c->C32, c->V32, c->T32, c->Z32);
+      gemm<float>(s, 'T', 'N', n, k, n, 0.5f, c->T32, n, c->V32, n, 0.f, c->Mt32, n);
+      gemm<float>(s, 'T', 'N', n, k, n, 0.5f, c->Z32, n, c->C32, n, 1.f, c->Mt32, n);
+      dmpt_dmu(s, n, k, c->Mt32, c->fill, o->kT, c->d_scal);
+      dmpt_response(s, n, k, c->Mt32, c->eig, c->fill, o->kT, c->d_scal);
+      gemm<float>(s, 'N', 'N', n, k, n, 1.f, c->C32, n, c->Mt32, n, 0.f, c->Zp32, n);
+      gemm<float>(s, 'N', 'T', n, n, k, 1.f, c->Zp32, n, c->C32, n, 0.f, c->A32, n, kCLower);
+      gemm<float>(s, 'N', 'T', n, n, k, 1.f, c->C32, n, c->Zp32, n, 1.f, c->A32, n, kCLower);
+      add_lower_f_sym_d(s, n, c->rho_ref, c->A32, c->rho);
+    } else if (form == kFormLow) {
       c->mixed_iters++;
       mark(c, kPhTransform);
       reduced_shift_f(s, g, c->L32, c->d_V, c->T32);
       gemm<float>(s, 'N', 'N', n, n, n, 1.f, c->Li32, n, c->T32, n, 0.f, c->C32, n, kALower | kBLower | kCLower);
       add_half_lower_f(s, n, c->A0_32, c->C32, c->A32);
       mark(c, kPhSytrd);
-      sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd);
+      sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd, c->d_status);
       mark(c, kPhStedc);
       if (stedc<float>(s, n, c->d32, c->e32, c->Z32, n, c->wk32_stedc, c->iwk_stedc, c->d_status) != 0)
         return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
@@ -680,11 +732,21 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       reduced_shift(s, g, c->Lc, c->d_V, c->T);
       dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
       add_half_lower(s, n, c->A0, c->C, c->H);
-      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true));
+      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true, /*all_vectors=*/mixed));
       k = (int)h_scal[kSNLevels];
       mark(c, kPhDensity);
       prof_flops(c, kPhDensity, (double)n * n * k);
       DG_CHECK(c, density(c, n, k, c->fill, c->rho));
+      if (mixed) {
+        // reference of the perturbative iterations: C (FP32), X = S C = L Y (FP32), rho, V
+        mark(c, kPhPert);
+        convert_d2f(s, (size_t)n * n, c->C, c->C32);
+        convert_d2f(s, (size_t)n * n, c->Z, c->Z32);
+        gemm<float>(s, 'N', 'N', n, n, n, 1.f, c->L32, n, c->Z32, n, 0.f, c->V32, n, kALower);
+        DG_CUDA(c, cudaMemcpyAsync(c->rho_ref, c->rho, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s));
+        DG_CUDA(c, cudaMemcpyAsync(c->Vref, c->d_V, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+        k_ref = k;
+      }
     }
     c->nlevels = k;
     mark(c, kPhMulliken);
@@ -701,16 +763,27 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     flush_marks(c);
     c->hist_e.push_back(h_scal[kSEnonScc] + h_scal[kSEscc]);
     c->hist_err.push_back(h_scal[kSErr]);
-    c->hist_prec.push_back(it_low ? DFTBGPU_PREC_MIXED : DFTBGPU_PREC_FP64);
+    c->hist_prec.push_back(it_form == kFormFull ? DFTBGPU_PREC_FP64
+                                                : (it_form == kFormLow ? DFTBGPU_PREC_MIXED : DFTBGPU_ITER_PERTURB));
     c->hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_it).count());
     conv = h_scal[kSConv] != 0.0;
     if (!conv && it != o->max_iter) ++mix_calls;
-    if (low && (conv || h_scal[kSErr] < switch_tol)) {
-      // converged or close enough in reduced precision: finish in FP64 (a converged FP32 state is
-      // re-evaluated, not accepted)
-      low = false;
-      conv = false;
-      continue;
+    if (mixed) {
+      if (form == kFormLow) {
+        // close enough in reduced precision (a converged FP32 state is re-evaluated, not accepted)
+        if (conv || h_scal[kSErr] < switch_tol) form = kFormFull;
+        conv = false;
+      } else if (form == kFormFull) {
+        if (!conv) {
+          form = kFormPert;
+          pert_run = 0;
+        }
+      } else {
+        // a converged perturbative state is re-evaluated by a FULL iteration at the same charges
+        // (the mixer leaves q_in unchanged on convergence); so is a long perturbative run
+        if (conv || ++pert_run >= kMaxPertRun) form = kFormFull;
+        conv = false;
+      }
     }
     if (conv) break;
   }
@@ -907,7 +980,7 @@ int dftbgpu_test_tridiag(dftbgpu_ctx *c, int n, const double *a, double *d, doub
   cudaStream_t s = c->stream;
   DG_CHECK(c, ensure_orbitals(c, n));
   DG_CUDA(c, cudaMemcpy(c->H, a, sizeof(double) * n * n, cudaMemcpyHostToDevice));
-  sytrd_lower(s, n, c->H, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd);
+  sytrd_lower(s, n, c->H, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd, c->d_status);
   DG_CUDA(c, cudaStreamSynchronize(s));
   DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));

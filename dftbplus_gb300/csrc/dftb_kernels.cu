@@ -511,6 +511,103 @@ void lower_f_to_sym_d(cudaStream_t s, int n, const float *A, double *B) {
   count_launch();
 }
 
+// ------------------------------------------------------------- density-matrix perturbation
+// First-order change of the density matrix of H C = S C eps under H -> H + 1/2 (S D + D S),
+// D = diag(dV): with X = S C (so C^T S C = I), M = C^T dH C = 1/2 (X^T D C + C^T D X) and
+// dP_ij = K_ij (M_ij - dmu delta_ij), K_ij = (f_i - f_j) / (eps_i - eps_j) (f' on the diagonal and
+// for degenerate pairs), drho = C dP C^T. Only rows/columns with f > 0 (i < k) contribute.
+__global__ void dmpt_scale_kernel(int n, const int *orb_atom, const double *V, const double *Vref,
+                                  const float *C, const float *X, float *DC, float *DX) {
+  const int j = blockIdx.y;
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x) {
+    const int a = orb_atom[l];
+    const float dv = (float)(V[a] - Vref[a]);
+    const size_t o = l + (size_t)j * n;
+    DC[o] = dv * C[o];
+    DX[o] = dv * X[o];
+  }
+}
+
+__device__ __forceinline__ double fermi_deriv(double f, double kT) {
+  // f = 2 / (1 + exp((e - mu) / kT))  =>  df/de = -f (2 - f) / (2 kT)
+  return -f * (2.0 - f) / (2.0 * kT);
+}
+
+__global__ void dmpt_dmu_kernel(int n, int k, const float *Mt, const double *fill, double kT, double *scal) {
+  __shared__ double sn[256], sd[256];
+  double num = 0.0, den = 0.0;
+  for (int i = threadIdx.x; i < k; i += 256) {
+    const double fp = fermi_deriv(fill[i], kT);
+    num = fma(fp, (double)Mt[i + (size_t)i * n], num);
+    den += fp;
+  }
+  sn[threadIdx.x] = num;
+  sd[threadIdx.x] = den;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sn[threadIdx.x] += sn[threadIdx.x + o];
+      sd[threadIdx.x] += sd[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scal[kSDmu] = (fabs(sd[0]) > 1e-300) ? sn[0] / sd[0] : 0.0;
+}
+
+__global__ void dmpt_response_kernel(int n, int k, float *Mt, const double *eig, const double *fill, double kT,
+                                     const double *scal) {
+  const int i = blockIdx.y;
+  const double fi = fill[i], ei = eig[i], dmu = scal[kSDmu];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const size_t o = j + (size_t)i * n;
+    double m = (double)Mt[o];
+    double K;
+    if (j == i) {
+      K = fermi_deriv(fi, kT);
+      m -= dmu;
+    } else {
+      const double de = ei - eig[j];
+      if (fabs(de) > 1e-9) K = (fi - fill[j]) / de;
+      else K = fermi_deriv(0.5 * (fi + fill[j]), kT);
+    }
+    double v = K * m;
+    if (j < k) v *= 0.5;
+    Mt[o] = (float)v;
+  }
+}
+
+__global__ void add_lower_f_sym_d_kernel(int n, const double *Bref, const float *D, double *B) {
+  const int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const size_t o = i + (size_t)j * n;
+    B[o] = Bref[o] + (double)((i >= j) ? D[o] : D[j + (size_t)i * n]);
+  }
+}
+
+void dmpt_scale(cudaStream_t s, const GeomDev &g, const double *V, const double *Vref, const float *C,
+                const float *X, float *DC, float *DX) {
+  const int *orb_atom = g.orb_off + g.natom + 1;
+  dim3 grid(std::min(ceil_div(g.norb, 256), 4), g.norb);
+  dmpt_scale_kernel<<<grid, 256, 0, s>>>(g.norb, orb_atom, V, Vref, C, X, DC, DX);
+  count_launch();
+}
+void dmpt_dmu(cudaStream_t s, int n, int k, const float *Mt, const double *fill, double kT, double *scal) {
+  dmpt_dmu_kernel<<<1, 256, 0, s>>>(n, k, Mt, fill, kT, scal);
+  count_launch();
+}
+void dmpt_response(cudaStream_t s, int n, int k, float *Mt, const double *eig, const double *fill, double kT,
+                   const double *scal) {
+  if (k <= 0) return;
+  dim3 grid(std::min(ceil_div(n, 256), 4), k);
+  dmpt_response_kernel<<<grid, 256, 0, s>>>(n, k, Mt, eig, fill, kT, scal);
+  count_launch();
+}
+void add_lower_f_sym_d(cudaStream_t s, int n, const double *Bref, const float *D, double *B) {
+  dim3 grid(std::min(ceil_div(n, 256), 4), n);
+  add_lower_f_sym_d_kernel<<<grid, 256, 0, s>>>(n, Bref, D, B);
+  count_launch();
+}
+
 void assemble_h(cudaStream_t s, const GeomDev &g, const double *H0, const double *S, const double *V,
                 double *H) {
   // orb_off holds natom+1 entries followed by norb orbital->atom entries (see api.cu)

@@ -23,7 +23,7 @@ struct GeomDev {
 // Device scalars written by the SCC kernels (index into a small double array).
 enum Scalar : int {
   kSEf = 0, kSEband, kSTS, kSE0, kSEnonScc, kSEscc, kSErep, kSErr, kSNel, kSConv,
-  kSNLevels, kSFermiStatus, kSCount = 16
+  kSNLevels, kSFermiStatus, kSDmu, kSCount = 16
 };
 
 // pair list
@@ -51,6 +51,18 @@ void add_half_lower_f(cudaStream_t s, int n, const float *A0, const float *B, fl
 void convert_d2f(cudaStream_t s, size_t n, const double *x, float *y);
 void convert_f2d(cudaStream_t s, size_t n, const float *x, double *y);
 void lower_f_to_sym_d(cudaStream_t s, int n, const float *A, double *B);
+// First-order density-matrix perturbation around a reference eigen-decomposition (mixed form):
+//   DC = diag(dV) C, DX = diag(dV) X with dV_l = V(atom l) - Vref(atom l)   (n x n, FP32)
+void dmpt_scale(cudaStream_t s, const GeomDev &g, const double *V, const double *Vref, const float *C,
+                const float *X, float *DC, float *DX);
+//   Fermi-level shift dmu = sum_i f'_i M_ii / sum_i f'_i over i < k (into scal[kSDmu]); Mt is n x k
+//   with Mt[j + i n] = M_ij
+void dmpt_dmu(cudaStream_t s, int n, int k, const float *Mt, const double *fill, double kT, double *scal);
+//   in place: Mt[j + i n] <- K_ij (M_ij - dmu delta_ij), halved for j < k (K = Fermi divided difference)
+void dmpt_response(cudaStream_t s, int n, int k, float *Mt, const double *eig, const double *fill, double kT,
+                   const double *scal);
+//   B = Bref + D with D symmetric from its lower triangle (FP32), B full
+void add_lower_f_sym_d(cudaStream_t s, int n, const double *Bref, const float *D, double *B);
 // Fermi filling (spin unpolarised) from ascending eigenvalues; writes fill[n], scal[...]
 void fermi_filling(cudaStream_t s, int n, const double *eig, double nel, double kT, double *fill,
                    double *scal);

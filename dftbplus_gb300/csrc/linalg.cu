@@ -445,10 +445,17 @@ void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int
 }
 
 // ------------------------------------------------------------------------------------- sytrd
-// Blocked lower tridiagonalisation with panel width PB (Householder vectors explicit in V).
+// Blocked lower tridiagonalisation (LAPACK dsytrd/dlatrd semantics: panel of PB reflectors with the
+// trailing-matrix update deferred to two rank-PB GEMMs per panel), Householder vectors explicit in V.
+//
+// All column steps of one panel run inside ONE cooperative (co-resident) kernel launch: the steps
+// of a column are separated by a grid barrier instead of a kernel boundary, so a panel costs one
+// launch and 4 barriers per column instead of 7 launches per column. Every reduction across CTAs
+// goes through per-CTA partials summed in a fixed order, so results are deterministic.
 constexpr int PB = 32;
-constexpr int ST = 64;        // symv tile
-constexpr int RED_THREADS = 1024;
+constexpr int ST = 64;                 // symv tile
+constexpr int kMaxPanelCtas = 4096;    // partial-sum slots per reduction
+constexpr unsigned kBarrierSpinLimit = 1u << 24;   // ~1.5 s of polling before a barrier gives up
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -475,103 +482,90 @@ __device__ T block_sum(T v, T *sh) {
   return r;
 }
 
-// Step 1a of column j (grid over rows): apply the panel's previous reflectors to A(j:n, j) and
-// write per-CTA partial sums of squares of A(j+2:n, j).
-template <typename T>
-__global__ void __launch_bounds__(256) latrd_update_kernel(int n, int j, int jj, T *A, int lda,
-                                                           const T *Vp, const T *Wp,
-                                                           T *part) {
-  __shared__ T sh[32];
-  __shared__ T coef[2 * PB];
-  const int t = threadIdx.x;
-  if (t < jj) {
-    coef[t] = Wp[j + (size_t)t * n];        // W(j, q)
-    coef[PB + t] = Vp[j + (size_t)t * n];   // V(j, q)
-  }
-  __syncthreads();
-  T *col = A + (size_t)j * lda;
-  T sig = T(0);
-  for (int r = j + blockIdx.x * blockDim.x + t; r < n; r += gridDim.x * blockDim.x) {
-    T a = col[r];
-    for (int q = 0; q < jj; ++q)
-      a -= Vp[r + (size_t)q * n] * coef[q] + Wp[r + (size_t)q * n] * coef[PB + q];
-    col[r] = a;
-    if (r >= j + 2) sig = fma(a, a, sig);
-  }
-  sig = block_sum<256>(sig, sh);
-  if (t == 0) part[blockIdx.x] = sig;
-}
+// Grid barrier state (zeroed before the first launch; the last arriver resets the counter).
+struct GridBar {
+  unsigned count, gen;
+  int err, pad;
+};
 
-// Step 1b (grid over rows): every CTA forms the same reflector from the partial sums (dlarfg
-// semantics: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta) and writes its rows of v.
-template <typename T>
-__global__ void __launch_bounds__(256) latrd_house_kernel(int n, int j, int jj, const T *A, int lda,
-                                                          const T *part, int nparts, T *Vp,
-                                                          T *V, int ldv, T *d, T *e,
-                                                          T *tau) {
-  __shared__ T s_scale;
-  const T *col = A + (size_t)j * lda;
+// Sense-by-generation grid barrier for a cooperative launch (all CTAs co-resident). Bounded: after
+// kBarrierSpinLimit polls the barrier records an error and stops waiting; once an error is recorded
+// no barrier waits any more, so a broken launch ends quickly with the error set.
+__device__ __forceinline__ void grid_sync(GridBar *b, unsigned nb) {
+  __syncthreads();
   if (threadIdx.x == 0) {
-    T sig = T(0);
-    for (int i = 0; i < nparts; ++i) sig += part[i];
-    T alpha = col[j + 1];
-    T beta, tv, scale;
-    if (sig == T(0)) {
-      tv = T(0);
-      beta = alpha;
-      scale = T(0);
-    } else {
-      beta = -copysign(sqrt(alpha * alpha + sig), alpha);
-      tv = (beta - alpha) / beta;
-      scale = T(1) / (alpha - beta);
-    }
-    s_scale = scale;
-    if (blockIdx.x == 0) {
-      d[j] = col[j];
-      e[j] = beta;
-      tau[j] = tv;
+    volatile unsigned *vgen = &b->gen;
+    volatile int *verr = &b->err;
+    if (*verr == 0) {
+      const unsigned g0 = *vgen;
+      __threadfence();
+      if (atomicAdd(&b->count, 1u) == nb - 1) {
+        atomicExch(&b->count, 0u);
+        __threadfence();
+        atomicAdd(&b->gen, 1u);
+      } else {
+        unsigned it = 0;
+        while (*vgen == g0) {
+          if (++it > kBarrierSpinLimit) {
+            atomicExch(&b->err, 1);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
     }
   }
   __syncthreads();
-  const T scale = s_scale;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    T v;
-    if (r <= j) v = T(0);
-    else if (r == j + 1) v = T(1);
-    else v = col[r] * scale;
-    Vp[r + (size_t)jj * n] = v;
-    V[r + (size_t)j * ldv] = v;
-  }
 }
 
-// y(j+1:n) = A22 v with A22 = A(j+1:n, j+1:n) read from its lower triangle only; partial sums per
-// 64x64 tile pair are reduced deterministically by symv_reduce_kernel.
 template <typename T>
-__global__ void __launch_bounds__(256) symv_partial_kernel(int m, int ntile, const T *A22, int lda,
-                                                           const T *v, T *P) {
-  __shared__ T tile[ST][ST + 1];
-  __shared__ T vr[ST], vc[ST];
-  // decode lower tile index -> (r, c), c <= r
-  int idx = blockIdx.x;
+struct PanelArgs {
+  T *A;
+  int lda, n, p0, nbp, ldv;
+  T *Vp, *Wp, *y, *P, *dots, *part, *wpart;
+  T *V, *d, *e, *tau;
+  GridBar *bar;
+  int *status;
+};
+
+// Sum of the G per-CTA partials p[0..G) in a fixed order (lane-strided, then a fixed shuffle tree);
+// every CTA gets the same value. Called by all threads; result valid in all threads.
+template <typename T>
+__device__ T sum_partials(const T *p, int G, T *sh) {
+  if (threadIdx.x < 32) {
+    T s = T(0);
+    for (int i = threadIdx.x; i < G; i += 32) s += __ldcg(p + i);
+    s = warp_sum(s);
+    if (threadIdx.x == 0) sh[0] = s;
+  }
+  __syncthreads();
+  T r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// One 64x64 lower tile (r, c) of A22 times v: row sums into P[r][c], and for c < r the transposed
+// product into P[c][r] (P[(tr * nt + tc) * ST + i] = partial of y(tr*ST + i) from tile column tc).
+template <typename T>
+__device__ void symv_tile(int idx, int m, int nt, const T *A22, int lda, const T *v, T *P,
+                          T (*tile)[ST + 1], T *vr, T *vc) {
   int r = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
   while ((r + 1) * (r + 2) / 2 <= idx) ++r;
   while (r * (r + 1) / 2 > idx) --r;
-  int c = idx - r * (r + 1) / 2;
+  const int c = idx - r * (r + 1) / 2;
   const int t = threadIdx.x;
   const int ri0 = r * ST, ci0 = c * ST;
   for (int k = t; k < ST * ST; k += 256) {
     int ii = k % ST, jj = k / ST;
     int gi = ri0 + ii, gj = ci0 + jj;
     T a = T(0);
-    if (gi < m && gj < m) {
-      if (r == c && ii < jj) a = T(0);  // filled by mirroring below
-      else a = A22[gi + (size_t)gj * lda];
-    }
+    if (gi < m && gj < m && !(r == c && ii < jj)) a = A22[gi + (size_t)gj * lda];
     tile[ii][jj] = a;
   }
   if (t < ST) {
-    vr[t] = (ri0 + t < m) ? v[ri0 + t] : T(0);
-    vc[t] = (ci0 + t < m) ? v[ci0 + t] : T(0);
+    vr[t] = (ri0 + t < m) ? __ldcg(v + ri0 + t) : T(0);
+    vc[t] = (ci0 + t < m) ? __ldcg(v + ci0 + t) : T(0);
   }
   __syncthreads();
   if (r == c) {
@@ -581,7 +575,6 @@ __global__ void __launch_bounds__(256) symv_partial_kernel(int m, int ntile, con
     }
     __syncthreads();
   }
-  // rows: 4 threads per row, each 16 columns
   {
     int row = t >> 2, part = t & 3;
     T s = T(0);
@@ -589,7 +582,7 @@ __global__ void __launch_bounds__(256) symv_partial_kernel(int m, int ntile, con
     for (int q = 0; q < 16; ++q) s = fma(tile[row][part * 16 + q], vc[part * 16 + q], s);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)r * ntile + c) * ST + row] = s;
+    if (part == 0) P[((size_t)r * nt + c) * ST + row] = s;
   }
   if (c < r) {
     int colq = t >> 2, part = t & 3;
@@ -598,78 +591,172 @@ __global__ void __launch_bounds__(256) symv_partial_kernel(int m, int ntile, con
     for (int q = 0; q < 16; ++q) s = fma(tile[part * 16 + q][colq], vr[part * 16 + q], s);
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)c * ntile + r) * ST + colq] = s;
-  }
-}
-
-template <typename T>
-__global__ void symv_reduce_kernel(int m, int ntile, const T *P, T *y) {
-  int r = blockIdx.x, i = threadIdx.x;
-  if (r * ST + i >= m) return;
-  T s = T(0);
-  for (int c = 0; c < ntile; ++c) s += P[((size_t)r * ntile + c) * ST + i];
-  y[r * ST + i] = s;
-}
-
-// dots[q] = W(:,q)^T v, dots[PB+q] = V(:,q)^T v over rows j+1..n-1 (one CTA per dot).
-template <typename T>
-__global__ void latrd_dots_kernel(int n, int j, int jj, const T *Vp, const T *Wp, T *dots) {
-  __shared__ T sh[32];
-  int q = blockIdx.x % jj;
-  bool isV = blockIdx.x >= jj;
-  const T *X = (isV ? Vp : Wp) + (size_t)q * n;
-  const T *v = Vp + (size_t)jj * n;
-  T s = T(0);
-  for (int r = j + 1 + threadIdx.x; r < n; r += 256) s = fma(X[r], v[r], s);
-  s = block_sum<256>(s, sh);
-  if (threadIdx.x == 0) dots[(isV ? PB : 0) + q] = s;
-}
-
-// w = tau (y - V (W^T v) - W (V^T v)); partial sums of w^T v per CTA.
-template <typename T>
-__global__ void latrd_w_kernel(int n, int j, int jj, const T *Vp, T *Wp, const T *y,
-                               const T *dots, const T *tau, T *part) {
-  __shared__ T sh[32];
-  __shared__ T cf[2 * PB];
-  if (threadIdx.x < jj) {
-    cf[threadIdx.x] = dots[threadIdx.x];
-    cf[PB + threadIdx.x] = dots[PB + threadIdx.x];
+    if (part == 0) P[((size_t)c * nt + r) * ST + colq] = s;
   }
   __syncthreads();
-  const T tv = tau[j];
-  const T *v = Vp + (size_t)jj * n;
-  T *w = Wp + (size_t)jj * n;
-  T s = T(0);
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    T val = T(0);
-    if (r > j) {
-      val = y[r];
-      for (int q = 0; q < jj; ++q)
-        val -= Vp[r + (size_t)q * n] * cf[q] + Wp[r + (size_t)q * n] * cf[PB + q];
-      val *= tv;
-      s = fma(val, v[r], s);
+}
+
+// One panel of the reduction (columns p0 .. p0+nbp-1). Per column j (index jj in the panel):
+//   U: finish W(:, jj-1) = w_raw + alpha v; A(j:n, j) -= V(j:n, 0:jj) W(j, 0:jj)^T + W V(j, :)^T;
+//      partial sums of squares of A(j+2:n, j)
+//   H: reflector (dlarfg: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta), v into Vp and V
+//   S: y = A22 v from the lower tiles of A22 = A(j+1:n, j+1:n); dots W(:,q)^T v and V(:,q)^T v
+//   W: w_raw = tau (y - V (W^T v) - W (V^T v)) (kept in y), partial sums of w_raw^T v
+// with alpha = -tau/2 w_raw^T v applied in the next U step (or after the last column).
+// Rows are handled by 8 lanes each (the q sums and the tile-column sum of y split over the lanes).
+template <typename T>
+__global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
+  __shared__ T tile[ST][ST + 1];
+  __shared__ T vr[ST], vc[ST];
+  __shared__ T sh[32];
+  __shared__ T cW[PB], cV[PB];
+  __shared__ T s_scal[4];
+  const int n = a.n, G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+  const int lane8 = t & 7, grp = (t >> 3) & 3;
+  const int wrow0 = (b * 256 + (t & ~31)) >> 3;    // 4 rows per warp, 8 lanes per row
+  const int rstride = (G * 256) >> 3;
+  const unsigned nb = (unsigned)G;
+  T alpha_prev = T(0);
+  for (int jj = 0; jj < a.nbp; ++jj) {
+    const int j = a.p0 + jj;
+    T *colj = a.A + (size_t)j * a.lda;
+    // ------------------------------------------------------------------ U
+    if (jj > 0) alpha_prev = T(-0.5) * __ldcg(a.tau + j - 1) * sum_partials(a.wpart, G, sh);
+    const T *vprev = a.Vp + (size_t)(jj - 1) * n;
+    if (t < jj) {
+      T w = __ldcg(a.Wp + j + (size_t)t * n);
+      if (t == jj - 1) w = __ldcg(a.y + j) + alpha_prev * __ldcg(vprev + j);
+      cW[t] = w;
+      cV[t] = __ldcg(a.Vp + j + (size_t)t * n);
     }
-    w[r] = val;
+    __syncthreads();
+    T sig = T(0);
+    for (int rb = wrow0; rb < n; rb += rstride) {   // warp-uniform trip count (shuffles below)
+      const int r = rb + grp;
+      T wq = T(0);
+      if (jj > 0 && r < n) {
+        wq = __ldcg(a.y + r) + alpha_prev * __ldcg(vprev + r);
+        if (lane8 == 0) a.Wp[r + (size_t)(jj - 1) * n] = wq;
+      }
+      const bool act = (r >= j && r < n);
+      T acc = T(0);
+      if (act) {
+        for (int q = lane8; q < jj; q += 8) {
+          const T wr = (q == jj - 1) ? wq : __ldcg(a.Wp + r + (size_t)q * n);
+          acc = fma(__ldcg(a.Vp + r + (size_t)q * n), cW[q], acc);
+          acc = fma(wr, cV[q], acc);
+        }
+      }
+      acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+      acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+      acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+      if (act && lane8 == 0) {
+        const T v = __ldcg(colj + r) - acc;
+        colj[r] = v;
+        if (r >= j + 2) sig = fma(v, v, sig);
+      }
+    }
+    sig = block_sum<256>(sig, sh);
+    if (t == 0) a.part[b] = sig;
+    grid_sync(a.bar, nb);
+    // ------------------------------------------------------------------ H
+    {
+      const T ss = sum_partials(a.part, G, sh);
+      if (t == 0) {
+        const T alpha = __ldcg(colj + j + 1);
+        T beta, tv, scale;
+        if (ss == T(0)) {
+          tv = T(0);
+          beta = alpha;
+          scale = T(0);
+        } else {
+          beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+          tv = (beta - alpha) / beta;
+          scale = T(1) / (alpha - beta);
+        }
+        s_scal[0] = scale;
+        if (b == 0) {
+          a.d[j] = __ldcg(colj + j);
+          a.e[j] = beta;
+          a.tau[j] = tv;
+        }
+      }
+      __syncthreads();
+      const T scale = s_scal[0];
+      for (int r = b * 256 + t; r < n; r += G * 256) {
+        T v;
+        if (r <= j) v = T(0);
+        else if (r == j + 1) v = T(1);
+        else v = __ldcg(colj + r) * scale;
+        a.Vp[r + (size_t)jj * n] = v;
+        a.V[r + (size_t)j * a.ldv] = v;
+      }
+    }
+    grid_sync(a.bar, nb);
+    // ------------------------------------------------------------------ S
+    const int m = n - j - 1;
+    const int nt = (m + ST - 1) / ST;
+    const T *v = a.Vp + (size_t)jj * n;
+    {
+      const int ntiles = nt * (nt + 1) / 2;
+      const T *A22 = a.A + (j + 1) + (size_t)(j + 1) * a.lda;
+      for (int idx = b; idx < ntiles; idx += G) symv_tile(idx, m, nt, A22, a.lda, v + j + 1, a.P, tile, vr, vc);
+      for (int dq = b; dq < 2 * jj; dq += G) {
+        const int q = dq % jj;
+        const bool isV = dq >= jj;
+        const T *X = (isV ? a.Vp : a.Wp) + (size_t)q * n;
+        T s = T(0);
+        for (int r = j + 1 + t; r < n; r += 256) s = fma(__ldcg(X + r), __ldcg(v + r), s);
+        s = block_sum<256>(s, sh);
+        if (t == 0) a.dots[(isV ? PB : 0) + q] = s;
+      }
+    }
+    grid_sync(a.bar, nb);
+    // ------------------------------------------------------------------ W
+    {
+      if (t < jj) {
+        cW[t] = __ldcg(a.dots + t);        // W(:,q)^T v
+        cV[t] = __ldcg(a.dots + PB + t);   // V(:,q)^T v
+      }
+      __syncthreads();
+      const T tv = __ldcg(a.tau + j);
+      T s = T(0);
+      for (int rb = wrow0; rb < n; rb += rstride) {   // warp-uniform trip count
+        const int r = rb + grp;
+        T acc = T(0);
+        if (r > j && r < n) {
+          const int rr = r - j - 1;
+          const T *Pr = a.P + (size_t)(rr / ST) * nt * ST + (rr % ST);
+          for (int c = lane8; c < nt; c += 8) acc += __ldcg(Pr + (size_t)c * ST);
+          for (int q = lane8; q < jj; q += 8) {
+            acc = fma(-__ldcg(a.Vp + r + (size_t)q * n), cW[q], acc);
+            acc = fma(-__ldcg(a.Wp + r + (size_t)q * n), cV[q], acc);
+          }
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        if (lane8 == 0 && r < n) {
+          const T val = (r > j) ? tv * acc : T(0);
+          a.y[r] = val;
+          s = fma(val, __ldcg(v + r), s);
+        }
+      }
+      s = block_sum<256>(s, sh);
+      if (t == 0) a.wpart[b] = s;
+    }
+    grid_sync(a.bar, nb);
   }
-  s = block_sum<256>(s, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-}
-
-template <typename T>
-__global__ void latrd_w2_kernel(int n, int j, int jj, const T *Vp, T *Wp, const T *tau,
-                                const T *part, int nparts) {
-  __shared__ T alpha;
-  if (threadIdx.x == 0) {
-    T s = T(0);
-    for (int i = 0; i < nparts; ++i) s += part[i];
-    alpha = T(-0.5) * tau[j] * s;
+  // finish the last column's W
+  {
+    const int jl = a.p0 + a.nbp - 1;
+    const T al = T(-0.5) * __ldcg(a.tau + jl) * sum_partials(a.wpart, G, sh);
+    const T *vl = a.Vp + (size_t)(a.nbp - 1) * n;
+    for (int r = b * 256 + t; r < n; r += G * 256)
+      a.Wp[r + (size_t)(a.nbp - 1) * n] = __ldcg(a.y + r) + al * __ldcg(vl + r);
   }
-  __syncthreads();
-  const T *v = Vp + (size_t)jj * n;
-  T *w = Wp + (size_t)jj * n;
-  T a = alpha;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-    if (r > j) w[r] = fma(a, v[r], w[r]);
+  if (t == 0 && a.status != nullptr && *(volatile int *)&a.bar->err != 0)
+    atomicMax(a.status, (int)kDevIterCap);
 }
 
 template <typename T>
@@ -680,11 +767,27 @@ __global__ void copy_last_diag_kernel(int n, const T *A, int lda, T *d) {
 template <typename T>
 size_t sytrd_work_size(int n) {
   size_t nt = (size_t)ceil_div(n, ST);
-  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 1024;
+  // Vp, Wp, y, P, dots, part, wpart, barrier (16 elements)
+  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 2 * (size_t)kMaxPanelCtas + 16;
+}
+
+// CTAs of the cooperative panel launch: every SM's resident share (at most 2 per SM).
+template <typename T>
+static int panel_ctas() {
+  static int g = 0;
+  if (g == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sytrd_panel_kernel<T>, 256, 0);
+    g = sms * std::max(1, std::min(per_sm, 2));
+    g = std::min(g, kMaxPanelCtas);
+  }
+  return g;
 }
 
 template <typename T>
-void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work) {
+void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work, int *status) {
   T *Vp = work;
   T *Wp = Vp + (size_t)n * PB;
   T *y = Wp + (size_t)n * PB;
@@ -692,35 +795,22 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
   size_t T0 = (size_t)ceil_div(n, ST);
   T *dots = P + T0 * T0 * ST;
   T *part = dots + 2 * PB;
+  T *wpart = part + kMaxPanelCtas;
+  GridBar *bar = reinterpret_cast<GridBar *>(wpart + kMaxPanelCtas);
   set_zero_t<T>(s, V, (size_t)ldv * n);
   if (n == 1) {
     copy_last_diag_kernel<T><<<1, 1, 0, s>>>(n, A, lda, d);
     count_launch();
     return;
   }
-  const int wblocks = std::min(ceil_div(n, 256), 64);
+  cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
+  const int G = panel_ctas<T>();
   for (int p0 = 0; p0 < n - 1; p0 += PB) {
     int nbp = std::min(PB, n - 1 - p0);
-    for (int jj = 0; jj < nbp; ++jj) {
-      int j = p0 + jj;
-      const int cb = std::min(ceil_div(n - j, 256), 64);
-      latrd_update_kernel<T><<<cb, 256, 0, s>>>(n, j, jj, A, lda, Vp, Wp, part);
-      latrd_house_kernel<T><<<cb, 256, 0, s>>>(n, j, jj, A, lda, part, cb, Vp, V, ldv, d, e, tau);
-      count_launch(2);
-      int m = n - j - 1;
-      int nt = ceil_div(m, ST);
-      const T *A22 = A + (j + 1) + (size_t)(j + 1) * lda;
-      symv_partial_kernel<T><<<nt * (nt + 1) / 2, 256, 0, s>>>(m, nt, A22, lda, Vp + (size_t)jj * n + j + 1, P);
-      symv_reduce_kernel<T><<<nt, ST, 0, s>>>(m, nt, P, y + j + 1);
-      count_launch(3);
-      if (jj > 0) {
-        latrd_dots_kernel<T><<<2 * jj, 256, 0, s>>>(n, j, jj, Vp, Wp, dots);
-        count_launch();
-      }
-      latrd_w_kernel<T><<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, y, dots, tau, part);
-      latrd_w2_kernel<T><<<wblocks, 256, 0, s>>>(n, j, jj, Vp, Wp, tau, part, wblocks);
-      count_launch(2);
-    }
+    PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, V, d, e, tau, bar, status};
+    void *args[] = {&pa};
+    cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
+    count_launch();
     int t0 = p0 + nbp;
     int m2 = n - t0;
     if (m2 > 0) {
@@ -793,8 +883,9 @@ void ormtr_left(cudaStream_t s, int n, int k, const T *V, int ldv, const T *tau,
 template size_t sytrd_work_size<double>(int);
 template size_t sytrd_work_size<float>(int);
 template void sytrd_lower<double>(cudaStream_t, int, double *, int, double *, double *, double *, double *, int,
-                                  double *);
-template void sytrd_lower<float>(cudaStream_t, int, float *, int, float *, float *, float *, float *, int, float *);
+                                  double *, int *);
+template void sytrd_lower<float>(cudaStream_t, int, float *, int, float *, float *, float *, float *, int, float *,
+                                 int *);
 template size_t ormtr_work_size<double>(int, int);
 template size_t ormtr_work_size<float>(int, int);
 template void ormtr_left<double>(cudaStream_t, int, int, const double *, int, const double *, double *, int,

@@ -47,11 +47,14 @@ void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int
 
 // Symmetric tridiagonal reduction A = Q T Q^T from the lower triangle of A (n x n, lda).
 // d[n], e[n-1], tau[n-1]; V (n x n, ldv) receives the Householder vectors explicitly
-// (column j: zeros for rows <= j, 1 at row j+1). work: sytrd_work_size<T>(n) elements.
+// (column j: zeros for rows <= j, 1 at row j+1). work: sytrd_work_size<T>(n) elements. Each panel
+// is one cooperative launch; if one of its bounded grid barriers gives up, *status (if given) is
+// raised to kDevIterCap.
 template <typename T>
 size_t sytrd_work_size(int n);
 template <typename T>
-void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work);
+void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work,
+                 int *status = nullptr);
 
 // Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: ormtr_work_size<T>(n, k).
 template <typename T>

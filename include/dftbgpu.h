@@ -34,9 +34,14 @@ enum {
   DFTBGPU_PREC_FP64 = 0,   /* plain FP64 drop-in */
   DFTBGPU_PREC_MIXED = 1   /* FP32 eigensolves (transform, tridiagonalisation, divide and conquer,
                               back-transformation, density matrix) for the early SCC iterations;
-                              Cholesky, Fermi filling, Mulliken, energies and mixing stay FP64;
-                              the cycle finishes and converges in FP64 */
+                              then one FP64 eigensolve with all eigenvectors, first-order
+                              density-matrix perturbation updates around it (FP32 GEMMs on the
+                              potential change), and FP64 again at the perturbatively converged
+                              charges. Cholesky, Fermi filling, Mulliken, energies and mixing stay
+                              FP64; the cycle only ends on a converged FP64 iteration */
 };
+/* Iteration kind recorded by dftbgpu_scc_history besides the two precision values above. */
+enum { DFTBGPU_ITER_PERTURB = 2 };
 
 typedef struct dftbgpu_ctx dftbgpu_ctx;
 
@@ -54,8 +59,8 @@ typedef struct {
   double net_charge;      /* Charge (e); N_el = sum(reference occupations) - net_charge */
   int precision;          /* DFTBGPU_PREC_* */
   int convergent_only;    /* ConvergentSCCOnly: return DFTBGPU_ERR_SCC_NOT_CONVERGED if 1 */
-  double mixed_switch_tol;/* mixed form: leave reduced precision once max|q_out - q_in| < this
-                             (0 = default 1e-4); the converged iteration is always FP64 */
+  double mixed_switch_tol;/* mixed form: leave the FP32 eigensolves once max|q_out - q_in| < this
+                             (0 = default 1e-3); the converged iteration is always FP64 */
 } dftbgpu_scc_opts;
 
 /* Energy terms as in dftb/energytypes.F90 (TEnergies) for this path. */
@@ -118,7 +123,8 @@ int dftbgpu_scc(dftbgpu_ctx *ctx, const dftbgpu_scc_opts *opts, const double *q_
  * reference prints (dftbplus/mainio.F90:4781-4845, printSccHeader/printSccInfo: iSCC, total
  * electronic energy, its change, SCC error): energy[i] = Eelec = EnonSCC + Escc of iteration i
  * (from its output charges), error[i] = max|q_out - q_in|,
- * precision[i] = DFTBGPU_PREC_FP64 or DFTBGPU_PREC_MIXED (an FP32 eigensolve), ms[i] = host wall
+ * precision[i] = DFTBGPU_PREC_FP64 (FP64 eigensolve), DFTBGPU_PREC_MIXED (FP32 eigensolve) or
+ * DFTBGPU_ITER_PERTURB (perturbative update around the last FP64 iteration), ms[i] = host wall
  * time of the iteration. Writes min(cap, count) entries (each array may be NULL) and returns the
  * iteration count, or -1 for a NULL context or cap < 0.
  */
@@ -159,10 +165,11 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  * reference's timer tree, common/environment.F90:97-133). Phases, in order:
  *   0 H0/S build + Cholesky, 1 potentials + H assembly, 2 L^-1 H L^-T, 3 tridiagonalisation,
  *   4 tridiagonal divide and conquer, 5 Fermi filling, 6 back-transformation (Q Z, L^-T Y),
- *   7 density matrix, 8 Mulliken + energies, 9 Broyden mixing, 10 gradients, 11 FP64 GEMM (all
- *   FP64 GEMM launches, overlapping the phases above), 12 FP32 GEMM (mixed form, likewise).
- * enable: 1 resets and starts accumulating, 0 stops. read: ms[13], flops[13] (algorithmic FLOPs
- * per phase as counted for the roofline), calls[13]; returns the number of phases written.
+ *   7 density matrix, 8 Mulliken + energies, 9 Broyden mixing, 10 gradients, 11 density-matrix
+ *   perturbation (mixed form: reference set-up and perturbative updates), 12 FP64 GEMM (all FP64
+ *   GEMM launches, overlapping the phases above), 13 FP32 GEMM (mixed form, likewise).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[14], flops[14] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[14]; returns the number of phases written.
  */
 int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);

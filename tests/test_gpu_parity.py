@@ -152,9 +152,10 @@ def test_spd_scc(gpu_lib, tio2_model):
 
 @pytest.mark.parametrize("n_mol,radius,seed", [(32, 10.0, 1), (128, 20.0, 128)])
 def test_mixed_precision_matches_fp64(gpu_lib, water_model, n_mol, radius, seed):
-    """Mixed form: FP32 eigensolves early, FP64 to convergence. Errors against the FP64 oracle must
-    meet the mixed targets (|dE| <= 1e-6 Ha/atom, max|dF| <= 1e-5 Ha/Bohr); in practice they are at
-    the SCC-tolerance level."""
+    """Mixed form: FP32 eigensolves early, one FP64 reference eigensolve, perturbative FP32 updates
+    around it, and a converged FP64 iteration at the end. Errors against the FP64 oracle must meet
+    the mixed targets (|dE| <= 1e-6 Ha/atom, max|dF| <= 1e-5 Ha/Bohr); the test holds them to the
+    SCC-tolerance level, which the form reaches."""
     from dftbplus_gb300 import binding, synth
     c, s = synth.water_cluster(n_mol, radius, seed)
     sys_ = O.System(water_model, c, s)
@@ -164,8 +165,13 @@ def test_mixed_precision_matches_fp64(gpu_lib, water_model, n_mol, radius, seed)
     res = ctx.scc(binding.default_opts(kT=1e-3, scc_tol=1e-7, precision=binding.PREC_MIXED))
     prof = ctx.profile_read()
     ctx.profile(False)
+    hist = ctx.scc_history()
     assert res["converged"]
     assert prof["gemm_fp32"]["calls"] > 0, "no reduced-precision iteration ran"
+    kinds = set(hist["precision"].tolist())
+    assert {binding.PREC_MIXED, binding.PREC_FP64, binding.ITER_PERTURB} <= kinds, kinds
+    assert hist["precision"][-1] == binding.PREC_FP64 and hist["error"][-1] < 1e-7
+    assert len(hist["error"]) == res["n_iter"]
     natom = len(s)
     de = abs(res["energies"]["EMermin"] - ref.energies["EMermin"])
     assert de / natom < 1e-8
