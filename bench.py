@@ -302,9 +302,11 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         ncpu = os.cpu_count() or 1
         t_it = cpu_scc_iteration_time(args.config)
-        cpu = {"value": 1.0 / (t_it * n_iter), "unit": "evals/s", "cores": ncpu, "kind": "port",
+        n_cpu = fp64["scc_iterations"] if fp64 else n_iter   # the CPU path is plain FP64
+        cpu = {"value": 1.0 / (t_it * n_cpu), "unit": "evals/s", "cores": ncpu, "kind": "port",
                "sample": f"one SCC iteration of the CPU oracle (LAPACK dsygvd via OpenBLAS, {ncpu} threads) "
-                         f"of {args.config} scaled by {n_iter} SCC iterations; gradients not timed"}
+                         f"of {args.config} scaled by the {n_cpu} SCC iterations of the FP64 cycle; "
+                         f"gradients not timed"}
     expected_iters = REF_SCC_ITERS.get(args.config)
     line = {"metric": METRIC, "precision": args.precision, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,

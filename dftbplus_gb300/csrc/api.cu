@@ -763,8 +763,9 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     flush_marks(c);
     c->hist_e.push_back(h_scal[kSEnonScc] + h_scal[kSEscc]);
     c->hist_err.push_back(h_scal[kSErr]);
-    c->hist_prec.push_back(it_form == kFormFull ? DFTBGPU_PREC_FP64
-                                                : (it_form == kFormLow ? DFTBGPU_PREC_MIXED : DFTBGPU_ITER_PERTURB));
+    c->hist_prec.push_back(it_form == kFormFull ? (int)DFTBGPU_PREC_FP64
+                                                : (it_form == kFormLow ? (int)DFTBGPU_PREC_MIXED
+                                                                       : (int)DFTBGPU_ITER_PERTURB));
     c->hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_it).count());
     conv = h_scal[kSConv] != 0.0;
     if (!conv && it != o->max_iter) ++mix_calls;

@@ -482,40 +482,38 @@ __device__ T block_sum(T v, T *sh) {
   return r;
 }
 
-// Grid barrier state (zeroed before the first launch; the last arriver resets the counter).
+// Grid barrier state, zeroed once per reduction: a monotonic arrival counter (barrier number e of
+// the reduction completes when count reaches (e + 1) * CTAs) and an error word.
 struct GridBar {
-  unsigned count, gen;
-  int err, pad;
+  unsigned count, pad0;
+  int err, pad1;
 };
 
-// Sense-by-generation grid barrier for a cooperative launch (all CTAs co-resident). Bounded: after
-// kBarrierSpinLimit polls the barrier records an error and stops waiting; once an error is recorded
-// no barrier waits any more, so a broken launch ends quickly with the error set.
-__device__ __forceinline__ void grid_sync(GridBar *b, unsigned nb) {
+// Grid barrier for a cooperative launch (all CTAs co-resident): one atomic arrival per CTA, then
+// poll until every CTA of this barrier number has arrived. Bounded: after kBarrierSpinLimit polls
+// it records an error and stops waiting; once an error is recorded no barrier waits any more, so a
+// broken launch ends quickly with the error set.
+__device__ __forceinline__ void grid_sync(GridBar *b, unsigned nb, unsigned &epoch) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned *vgen = &b->gen;
     volatile int *verr = &b->err;
     if (*verr == 0) {
-      const unsigned g0 = *vgen;
       __threadfence();
-      if (atomicAdd(&b->count, 1u) == nb - 1) {
-        atomicExch(&b->count, 0u);
-        __threadfence();
-        atomicAdd(&b->gen, 1u);
-      } else {
-        unsigned it = 0;
-        while (*vgen == g0) {
-          if (++it > kBarrierSpinLimit) {
-            atomicExch(&b->err, 1);
-            break;
-          }
-          __nanosleep(64);
+      atomicAdd(&b->count, 1u);
+      const unsigned target = (epoch + 1u) * nb;
+      volatile unsigned *vc = &b->count;
+      unsigned it = 0;
+      while ((int)(*vc - target) < 0) {
+        if (++it > kBarrierSpinLimit) {
+          atomicExch(&b->err, 1);
+          break;
         }
+        __nanosleep(20);
       }
       __threadfence();
     }
   }
+  ++epoch;
   __syncthreads();
 }
 
@@ -523,9 +521,10 @@ template <typename T>
 struct PanelArgs {
   T *A;
   int lda, n, p0, nbp, ldv;
-  T *Vp, *Wp, *y, *P, *dots, *part, *wpart;
+  T *Vp, *Wp, *y, *P, *dots, *part, *wpart, *dpart;
   T *V, *d, *e, *tau;
   GridBar *bar;
+  unsigned epoch0;   // barriers completed by earlier panels of this reduction
   int *status;
 };
 
@@ -545,65 +544,33 @@ __device__ T sum_partials(const T *p, int G, T *sh) {
   return r;
 }
 
-// One 64x64 lower tile (r, c) of A22 times v: row sums into P[r][c], and for c < r the transposed
-// product into P[c][r] (P[(tr * nt + tc) * ST + i] = partial of y(tr*ST + i) from tile column tc).
-template <typename T>
-__device__ void symv_tile(int idx, int m, int nt, const T *A22, int lda, const T *v, T *P,
-                          T (*tile)[ST + 1], T *vr, T *vc) {
-  int r = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
+// Decode a lower-triangle tile index into (row tile r, column tile c), c <= r.
+__device__ __forceinline__ void tile_rc(int idx, int &r, int &c) {
+  // single-precision estimate (FP64 is a slow pipe here), made exact by the integer corrections
+  r = (int)((sqrtf(8.f * (float)idx + 1.f) - 1.f) * 0.5f);
   while ((r + 1) * (r + 2) / 2 <= idx) ++r;
   while (r * (r + 1) / 2 > idx) --r;
-  const int c = idx - r * (r + 1) / 2;
-  const int t = threadIdx.x;
-  const int ri0 = r * ST, ci0 = c * ST;
-  for (int k = t; k < ST * ST; k += 256) {
-    int ii = k % ST, jj = k / ST;
-    int gi = ri0 + ii, gj = ci0 + jj;
-    T a = T(0);
-    if (gi < m && gj < m && !(r == c && ii < jj)) a = A22[gi + (size_t)gj * lda];
-    tile[ii][jj] = a;
-  }
-  if (t < ST) {
-    vr[t] = (ri0 + t < m) ? __ldcg(v + ri0 + t) : T(0);
-    vc[t] = (ci0 + t < m) ? __ldcg(v + ci0 + t) : T(0);
-  }
-  __syncthreads();
-  if (r == c) {
-    for (int k = t; k < ST * ST; k += 256) {
-      int ii = k % ST, jj = k / ST;
-      if (ii < jj) tile[ii][jj] = tile[jj][ii];
-    }
-    __syncthreads();
-  }
-  {
-    int row = t >> 2, part = t & 3;
-    T s = T(0);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) s = fma(tile[row][part * 16 + q], vc[part * 16 + q], s);
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)r * nt + c) * ST + row] = s;
-  }
-  if (c < r) {
-    int colq = t >> 2, part = t & 3;
-    T s = T(0);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) s = fma(tile[part * 16 + q][colq], vr[part * 16 + q], s);
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (part == 0) P[((size_t)c * nt + r) * ST + colq] = s;
-  }
-  __syncthreads();
+  c = idx - r * (r + 1) / 2;
+}
+
+// Element v(r) of the current reflector (absolute row r) from the updated column j: 0 above the
+// subdiagonal, 1 on it, A(r, j) * scale below (every CTA forms it from the same data).
+template <typename T>
+__device__ __forceinline__ T reflector_elem(const T *colj, int j, int r, T scale) {
+  return (r <= j) ? T(0) : ((r == j + 1) ? T(1) : __ldcg(colj + r) * scale);
 }
 
 // One panel of the reduction (columns p0 .. p0+nbp-1). Per column j (index jj in the panel):
-//   U: finish W(:, jj-1) = w_raw + alpha v; A(j:n, j) -= V(j:n, 0:jj) W(j, 0:jj)^T + W V(j, :)^T;
+//   A: finish W(:, jj-1) = w_raw + alpha v; A(j:n, j) -= V(j:n, 0:jj) W(j, 0:jj)^T + W V(j, :)^T;
 //      partial sums of squares of A(j+2:n, j)
-//   H: reflector (dlarfg: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta), v into Vp and V
-//   S: y = A22 v from the lower tiles of A22 = A(j+1:n, j+1:n); dots W(:,q)^T v and V(:,q)^T v
-//   W: w_raw = tau (y - V (W^T v) - W (V^T v)) (kept in y), partial sums of w_raw^T v
-// with alpha = -tau/2 w_raw^T v applied in the next U step (or after the last column).
-// Rows are handled by 8 lanes each (the q sums and the tile-column sum of y split over the lanes).
+//   B: reflector (dlarfg: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta) formed by every
+//      CTA from the partial sums; v stored; y = A22 v from 64x64 lower tiles of A22 = A(j+1:n, j+1:n)
+//      (tiles double-buffered through registers) with v read from column j on the fly; dots
+//      W(:,q)^T v and V(:,q)^T v
+//   C: w_raw = tau (y - V (W^T v) - W (V^T v)) (kept in y), partial sums of w_raw^T v
+// with alpha = -tau/2 w_raw^T v applied in the next A step (or after the last column). Three grid
+// barriers per column. Rows are handled by 8 lanes each (the q sums and the tile-column sum of y
+// split over the lanes, combined by a fixed shuffle tree).
 template <typename T>
 __global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
   __shared__ T tile[ST][ST + 1];
@@ -616,11 +583,13 @@ __global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
   const int wrow0 = (b * 256 + (t & ~31)) >> 3;    // 4 rows per warp, 8 lanes per row
   const int rstride = (G * 256) >> 3;
   const unsigned nb = (unsigned)G;
+  unsigned epoch = a.epoch0;
   T alpha_prev = T(0);
+  T *red = &tile[0][0];   // phase-A scratch (the tile is only used in phase B)
   for (int jj = 0; jj < a.nbp; ++jj) {
     const int j = a.p0 + jj;
     T *colj = a.A + (size_t)j * a.lda;
-    // ------------------------------------------------------------------ U
+    // ------------------------------------------------------------------ A
     if (jj > 0) alpha_prev = T(-0.5) * __ldcg(a.tau + j - 1) * sum_partials(a.wpart, G, sh);
     const T *vprev = a.Vp + (size_t)(jj - 1) * n;
     if (t < jj) {
@@ -631,35 +600,72 @@ __global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
     }
     __syncthreads();
     T sig = T(0);
+    T pdv[4] = {T(0), T(0), T(0), T(0)}, pdw[4] = {T(0), T(0), T(0), T(0)};   // V/W(r, q) A(r, j), r >= j+2
     for (int rb = wrow0; rb < n; rb += rstride) {   // warp-uniform trip count (shuffles below)
       const int r = rb + grp;
-      T wq = T(0);
-      if (jj > 0 && r < n) {
-        wq = __ldcg(a.y + r) + alpha_prev * __ldcg(vprev + r);
-        if (lane8 == 0) a.Wp[r + (size_t)(jj - 1) * n] = wq;
+      const bool in = r < n, act = in && r >= j;
+      // issue every load of the row first
+      T yv = T(0), vp = T(0), cj = T(0), vq[4], wv[4];
+      if (jj > 0 && in) {
+        yv = __ldcg(a.y + r);
+        vp = __ldcg(vprev + r);
       }
-      const bool act = (r >= j && r < n);
+      if (act) cj = __ldcg(colj + r);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = lane8 + 8 * i;
+        const bool use = act && q < jj;
+        vq[i] = use ? __ldcg(a.Vp + r + (size_t)q * n) : T(0);
+        wv[i] = (use && q != jj - 1) ? __ldcg(a.Wp + r + (size_t)q * n) : T(0);
+      }
+      const T wq = yv + alpha_prev * vp;
+      if (jj > 0 && in && lane8 == 0) a.Wp[r + (size_t)(jj - 1) * n] = wq;
       T acc = T(0);
-      if (act) {
-        for (int q = lane8; q < jj; q += 8) {
-          const T wr = (q == jj - 1) ? wq : __ldcg(a.Wp + r + (size_t)q * n);
-          acc = fma(__ldcg(a.Vp + r + (size_t)q * n), cW[q], acc);
-          acc = fma(wr, cV[q], acc);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = lane8 + 8 * i;
+        if (act && q < jj) {
+          acc = fma(vq[i], cW[q], acc);
+          acc = fma((q == jj - 1) ? wq : wv[i], cV[q], acc);
         }
       }
       acc += __shfl_xor_sync(0xffffffffu, acc, 4);
       acc += __shfl_xor_sync(0xffffffffu, acc, 2);
       acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+      const T ar = cj - acc;   // updated A(r, j), identical in the 8 lanes
       if (act && lane8 == 0) {
-        const T v = __ldcg(colj + r) - acc;
-        colj[r] = v;
-        if (r >= j + 2) sig = fma(v, v, sig);
+        colj[r] = ar;
+        if (r >= j + 2) sig = fma(ar, ar, sig);
+      }
+      if (act && r >= j + 2) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          pdv[i] = fma(vq[i], ar, pdv[i]);
+          pdw[i] = fma((lane8 + 8 * i == jj - 1) ? wq : wv[i], ar, pdw[i]);
+        }
+      }
+    }
+    // per-CTA partials of the dots (fixed-order sum over the CTA's 32 row groups)
+    if (jj > 0) {
+      const int g32 = t >> 3;   // row group 0..31 of this CTA
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        red[g32 * 2 * PB + lane8 + 8 * i] = pdw[i];
+        red[g32 * 2 * PB + PB + lane8 + 8 * i] = pdv[i];
+      }
+      __syncthreads();
+      if (t < 2 * PB) {
+        T sacc = T(0);
+        for (int g2 = 0; g2 < 32; ++g2) sacc += red[g2 * 2 * PB + t];
+        a.dpart[(size_t)b * 2 * PB + t] = sacc;
       }
     }
     sig = block_sum<256>(sig, sh);
     if (t == 0) a.part[b] = sig;
-    grid_sync(a.bar, nb);
-    // ------------------------------------------------------------------ H
+    grid_sync(a.bar, nb, epoch);
+    // ------------------------------------------------------------------ B
+    const int m = n - j - 1;
+    const int nt = (m + ST - 1) / ST;
     {
       const T ss = sum_partials(a.part, G, sh);
       if (t == 0) {
@@ -684,35 +690,85 @@ __global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
       __syncthreads();
       const T scale = s_scal[0];
       for (int r = b * 256 + t; r < n; r += G * 256) {
-        T v;
-        if (r <= j) v = T(0);
-        else if (r == j + 1) v = T(1);
-        else v = __ldcg(colj + r) * scale;
+        const T v = reflector_elem(colj, j, r, scale);
         a.Vp[r + (size_t)jj * n] = v;
         a.V[r + (size_t)j * a.ldv] = v;
       }
-    }
-    grid_sync(a.bar, nb);
-    // ------------------------------------------------------------------ S
-    const int m = n - j - 1;
-    const int nt = (m + ST - 1) / ST;
-    const T *v = a.Vp + (size_t)jj * n;
-    {
+      // y = A22 v, tile by tile; the next tile's elements are loaded while this one is reduced
       const int ntiles = nt * (nt + 1) / 2;
       const T *A22 = a.A + (j + 1) + (size_t)(j + 1) * a.lda;
-      for (int idx = b; idx < ntiles; idx += G) symv_tile(idx, m, nt, A22, a.lda, v + j + 1, a.P, tile, vr, vc);
+      const int ii = t & (ST - 1), jc = t >> 6;   // element (ii, jc + 4 q) of a tile, q < 16
+      T reg[16], rv = T(0), cvv = T(0);
+      int r = 0, c = 0;
+      auto load_tile = [&](int idx) {
+        tile_rc(idx, r, c);
+        const int gi = r * ST + ii;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int jt = jc + 4 * q, gj = c * ST + jt;
+          reg[q] = (gi < m && gj < m && !(r == c && ii < jt)) ? A22[gi + (size_t)gj * a.lda] : T(0);
+        }
+        if (t < ST) {
+          rv = (r * ST + t < m) ? reflector_elem(colj, j, j + 1 + r * ST + t, scale) : T(0);
+          cvv = (c * ST + t < m) ? reflector_elem(colj, j, j + 1 + c * ST + t, scale) : T(0);
+        }
+      };
+      int idx = b;
+      if (idx < ntiles) load_tile(idx);
+      // dots W(:,q)^T v and V(:,q)^T v = scale * sum_{r >= j+2} X(r, q) A(r, j) + X(j+1, q)
       for (int dq = b; dq < 2 * jj; dq += G) {
         const int q = dq % jj;
         const bool isV = dq >= jj;
-        const T *X = (isV ? a.Vp : a.Wp) + (size_t)q * n;
-        T s = T(0);
-        for (int r = j + 1 + t; r < n; r += 256) s = fma(__ldcg(X + r), __ldcg(v + r), s);
-        s = block_sum<256>(s, sh);
-        if (t == 0) a.dots[(isV ? PB : 0) + q] = s;
+        T s2 = T(0);
+        for (int b2 = t; b2 < G; b2 += 256) s2 += __ldcg(a.dpart + (size_t)b2 * 2 * PB + (isV ? PB : 0) + q);
+        s2 = block_sum<256>(s2, sh);
+        if (t == 0) {
+          const T x1 = __ldcg((isV ? a.Vp : a.Wp) + (j + 1) + (size_t)q * n);
+          a.dots[(isV ? PB : 0) + q] = scale * s2 + x1;
+        }
+      }
+      while (idx < ntiles) {
+        const int tr = r, tc = c;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tile[ii][jc + 4 * q] = reg[q];
+        if (t < ST) {
+          vr[t] = rv;
+          vc[t] = cvv;
+        }
+        __syncthreads();
+        const int nidx = idx + G;
+        if (nidx < ntiles) load_tile(nidx);
+        if (tr == tc) {
+          for (int k = t; k < ST * ST; k += 256) {
+            const int i2 = k % ST, j2 = k / ST;
+            if (i2 < j2) tile[i2][j2] = tile[j2][i2];
+          }
+          __syncthreads();
+        }
+        {
+          const int row = t >> 2, part = t & 3;
+          T s = T(0);
+#pragma unroll
+          for (int q = 0; q < 16; ++q) s = fma(tile[row][part * 16 + q], vc[part * 16 + q], s);
+          s += __shfl_xor_sync(0xffffffffu, s, 1);
+          s += __shfl_xor_sync(0xffffffffu, s, 2);
+          if (part == 0) a.P[((size_t)tr * nt + tc) * ST + row] = s;
+        }
+        if (tc < tr) {
+          const int colq = t >> 2, part = t & 3;
+          T s = T(0);
+#pragma unroll
+          for (int q = 0; q < 16; ++q) s = fma(tile[part * 16 + q][colq], vr[part * 16 + q], s);
+          s += __shfl_xor_sync(0xffffffffu, s, 1);
+          s += __shfl_xor_sync(0xffffffffu, s, 2);
+          if (part == 0) a.P[((size_t)tc * nt + tr) * ST + colq] = s;
+        }
+        __syncthreads();
+        idx = nidx;
       }
     }
-    grid_sync(a.bar, nb);
-    // ------------------------------------------------------------------ W
+    grid_sync(a.bar, nb, epoch);
+    // ------------------------------------------------------------------ C
     {
       if (t < jj) {
         cW[t] = __ldcg(a.dots + t);        // W(:,q)^T v
@@ -720,32 +776,47 @@ __global__ void __launch_bounds__(256) sytrd_panel_kernel(PanelArgs<T> a) {
       }
       __syncthreads();
       const T tv = __ldcg(a.tau + j);
+      const T *v = a.Vp + (size_t)jj * n;
       T s = T(0);
       for (int rb = wrow0; rb < n; rb += rstride) {   // warp-uniform trip count
         const int r = rb + grp;
-        T acc = T(0);
-        if (r > j && r < n) {
+        const bool act = r > j && r < n;
+        T acc = T(0), vrow = T(0), vq[4], wv[4];
+        if (act) {
+          vrow = __ldcg(v + r);
           const int rr = r - j - 1;
           const T *Pr = a.P + (size_t)(rr / ST) * nt * ST + (rr % ST);
-          for (int c = lane8; c < nt; c += 8) acc += __ldcg(Pr + (size_t)c * ST);
-          for (int q = lane8; q < jj; q += 8) {
-            acc = fma(-__ldcg(a.Vp + r + (size_t)q * n), cW[q], acc);
-            acc = fma(-__ldcg(a.Wp + r + (size_t)q * n), cV[q], acc);
+#pragma unroll 4
+          for (int c2 = lane8; c2 < nt; c2 += 8) acc += __ldcg(Pr + (size_t)c2 * ST);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = lane8 + 8 * i;
+          const bool use = act && q < jj;
+          vq[i] = use ? __ldcg(a.Vp + r + (size_t)q * n) : T(0);
+          wv[i] = use ? __ldcg(a.Wp + r + (size_t)q * n) : T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = lane8 + 8 * i;
+          if (act && q < jj) {
+            acc = fma(-vq[i], cW[q], acc);
+            acc = fma(-wv[i], cV[q], acc);
           }
         }
         acc += __shfl_xor_sync(0xffffffffu, acc, 4);
         acc += __shfl_xor_sync(0xffffffffu, acc, 2);
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
         if (lane8 == 0 && r < n) {
-          const T val = (r > j) ? tv * acc : T(0);
+          const T val = act ? tv * acc : T(0);
           a.y[r] = val;
-          s = fma(val, __ldcg(v + r), s);
+          s = fma(val, vrow, s);
         }
       }
       s = block_sum<256>(s, sh);
       if (t == 0) a.wpart[b] = s;
     }
-    grid_sync(a.bar, nb);
+    grid_sync(a.bar, nb, epoch);
   }
   // finish the last column's W
   {
@@ -767,8 +838,9 @@ __global__ void copy_last_diag_kernel(int n, const T *A, int lda, T *d) {
 template <typename T>
 size_t sytrd_work_size(int n) {
   size_t nt = (size_t)ceil_div(n, ST);
-  // Vp, Wp, y, P, dots, part, wpart, barrier (16 elements)
-  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 2 * (size_t)kMaxPanelCtas + 16;
+  // Vp, Wp, y, P, dots, part, wpart, dpart, barrier (16 elements)
+  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 2 * (size_t)kMaxPanelCtas +
+         2 * (size_t)PB * kMaxPanelCtas + 16;
 }
 
 // CTAs of the cooperative panel launch: every SM's resident share (at most 2 per SM).
@@ -796,7 +868,8 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
   T *dots = P + T0 * T0 * ST;
   T *part = dots + 2 * PB;
   T *wpart = part + kMaxPanelCtas;
-  GridBar *bar = reinterpret_cast<GridBar *>(wpart + kMaxPanelCtas);
+  T *dpart = wpart + kMaxPanelCtas;
+  GridBar *bar = reinterpret_cast<GridBar *>(dpart + 2 * (size_t)PB * kMaxPanelCtas);
   set_zero_t<T>(s, V, (size_t)ldv * n);
   if (n == 1) {
     copy_last_diag_kernel<T><<<1, 1, 0, s>>>(n, A, lda, d);
@@ -805,9 +878,11 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
   }
   cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
   const int G = panel_ctas<T>();
+  unsigned epoch0 = 0;
   for (int p0 = 0; p0 < n - 1; p0 += PB) {
     int nbp = std::min(PB, n - 1 - p0);
-    PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, V, d, e, tau, bar, status};
+    PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, dpart, V, d, e, tau, bar, epoch0, status};
+    epoch0 += 3u * (unsigned)nbp;
     void *args[] = {&pa};
     cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
     count_launch();
