@@ -57,6 +57,9 @@ SIGNATURES = {
     "dftbgpu_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), _dp, C.POINTER(Energies), _dp, _dp, _dp, _dp, _ip, _ip]),
     "dftbgpu_scc_history": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip, _dp]),
     "dftbgpu_gradients": (C.c_int, [C.c_void_p, _dp]),
+    "dftbgpu_batch_set_geometries": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip]),
+    "dftbgpu_batch_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), C.c_void_p, _dp, _ip, _ip]),
+    "dftbgpu_batch_gradients": (C.c_int, [C.c_void_p, _dp]),
     "dftbgpu_gradients_dev": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dftbgpu_n_orbitals": (C.c_int, [C.c_void_p, _ip]),
     "dftbgpu_get_orbital_populations": (C.c_int, [C.c_void_p, _dp]),
@@ -216,6 +219,36 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dftbgpu_kernel_launches(self.h))
+
+    # -------------------------------------------------------------- batched form
+    def batch_set_geometries(self, coords_list, species_list):
+        """Many independent molecules: coords_list[i] is (3, nat_i) in Bohr, species_list[i] (nat_i,)."""
+        off = np.zeros(len(coords_list) + 1, dtype=np.int32)
+        off[1:] = np.cumsum([len(sp) for sp in species_list])
+        xyz = np.ascontiguousarray(np.concatenate([np.asarray(c).T for c in coords_list]), dtype=np.float64)
+        sp = np.ascontiguousarray(np.concatenate(species_list), dtype=np.int32)
+        self.check(self.lib.dftbgpu_batch_set_geometries(self.h, len(coords_list), _p(off, C.c_int),
+                                                         _p(xyz, C.c_double), _p(sp, C.c_int)))
+        self.batch_atom_off = off
+        return off
+
+    def batch_scc(self, opts: SccOpts):
+        nmol = len(self.batch_atom_off) - 1
+        en = (Energies * nmol)()
+        qout = np.zeros(int(self.batch_atom_off[-1]))
+        nit = np.zeros(nmol, dtype=np.int32)
+        conv = np.zeros(nmol, dtype=np.int32)
+        self.check(self.lib.dftbgpu_batch_scc(self.h, C.byref(opts), C.cast(en, C.c_void_p), _p(qout, C.c_double),
+                                              _p(nit, C.c_int), _p(conv, C.c_int)))
+        return dict(energies=[e.as_dict() for e in en], q_out=qout, n_iter=nit, converged=conv.astype(bool))
+
+    def batch_gradients(self):
+        """Energy gradients per molecule, list of (3, nat_i) arrays."""
+        off = self.batch_atom_off
+        g = np.zeros(3 * int(off[-1]))
+        self.check(self.lib.dftbgpu_batch_gradients(self.h, _p(g, C.c_double)))
+        g = g.reshape(-1, 3).T
+        return [g[:, off[i]:off[i + 1]].copy() for i in range(len(off) - 1)]
 
     def scc_history(self) -> dict:
         """Per-iteration record of the last SCC call: electronic energy, SCC error, precision form

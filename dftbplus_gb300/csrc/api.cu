@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "batch.cuh"
 #include "dftb_kernels.cuh"
 #include "linalg.cuh"
 
@@ -63,6 +64,8 @@ struct Ctx {
   double *rho_ref = nullptr, *Vref = nullptr;
   // per-iteration record of the last SCC call: electronic energy, max|q_out - q_in|, precision, host ms
   std::vector<double> hist_e, hist_err, hist_ms;
+  // batched form (many independent molecules sharing the model)
+  BatchState *batch = nullptr;
   std::vector<int> hist_prec;
   double *eig = nullptr, *fill = nullptr, *fe = nullptr, *dd = nullptr, *ee = nullptr, *tau = nullptr,
          *qorb = nullptr, *eorb = nullptr;
@@ -432,6 +435,10 @@ int dftbgpu_destroy(dftbgpu_ctx *c) {
                   c->wk32_stedc, c->Mt32, c->Zp32, c->rho_ref, c->Vref};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (c->batch) {
+    batch_free(*c->batch);
+    delete c->batch;
+  }
   cudaStreamDestroy(c->stream);
   delete c;
   return DFTBGPU_OK;
@@ -1005,6 +1012,90 @@ int dftbgpu_test_stedc(dftbgpu_ctx *c, int n, double *d, const double *e, double
   DG_CUDA(c, cudaMemcpy(q, c->Z, sizeof(double) * n * n, cudaMemcpyDeviceToHost));
   c->have_geom = false;
   c->have_scc = false;
+  return DFTBGPU_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------ batched form
+extern "C" {
+
+int dftbgpu_batch_set_geometries(dftbgpu_ctx *c, int nmol, const int *atom_off, const double *coords,
+                                 const int *species) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (!c->have_model) return set_error(c, DFTBGPU_ERR_STATE, "batch: no model set");
+  cudaSetDevice(c->device);
+  if (!c->batch) c->batch = new BatchState();
+  char msg[256] = {0};
+  const int rc = batch_set_geometries(c->stream, *c->batch, model_view(c), c->h_sp, c->sk_cut_max, nmol, atom_off,
+                                      coords, species, false, msg, sizeof(msg));
+  if (rc != DFTBGPU_OK) return set_error(c, rc, "%s", msg);
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_batch_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, dftbgpu_energies *energies, double *q_out,
+                      int *n_iter, int *converged) {
+  if (!c || !o) return DFTBGPU_ERR_ARGS;
+  if (!c->batch || !c->batch->have_geom) return set_error(c, DFTBGPU_ERR_STATE, "batch: no geometries set");
+  if (o->max_iter < 1 || o->max_iter > 150) return set_error(c, DFTBGPU_ERR_ARGS, "scc: max_iter must be in 1..150");
+  if (!(o->kT > 0.0)) return set_error(c, DFTBGPU_ERR_ARGS, "scc: kT must be > 0 (Fermi filling)");
+  if (o->precision != DFTBGPU_PREC_FP64 && o->precision != DFTBGPU_PREC_MIXED)
+    return set_error(c, DFTBGPU_ERR_ARGS, "scc: unknown precision form %d", o->precision);
+  cudaSetDevice(c->device);
+  BatchState &b = *c->batch;
+  BatchOpts bo{o->kT, o->scc_tol, o->mix_alpha, o->mix_omega0, o->mix_min_weight, o->mix_max_weight,
+               o->mix_weight_fac, o->net_charge, (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 1e-3,
+               o->max_iter, o->min_iter, o->precision == DFTBGPU_PREC_MIXED ? 1 : 0};
+  char msg[256] = {0};
+  int rc = batch_scc(c->stream, b, model_view(c), bo, msg, sizeof(msg));
+  if (rc != DFTBGPU_OK) return set_error(c, rc, "%s", msg);
+  std::vector<MolState> st(b.nmol);
+  DG_CUDA(c, cudaMemcpy(st.data(), b.d.st, sizeof(MolState) * b.nmol, cudaMemcpyDeviceToHost));
+  if (q_out) DG_CUDA(c, cudaMemcpy(q_out, b.d.qout, sizeof(double) * b.natom, cudaMemcpyDeviceToHost));
+  int first_bad = -1, bad_status = 0, first_unconv = -1;
+  for (int i = 0; i < b.nmol; ++i) {
+    const MolState &m = st[i];
+    if (energies) {
+      dftbgpu_energies &e = energies[i];
+      e.EnonSCC = m.enonscc;
+      e.Escc = m.escc;
+      e.Erep = m.erep;
+      e.Eband = m.eband;
+      e.TS = m.ts;
+      e.E0 = m.e0;
+      e.Etotal = m.enonscc + m.escc + m.erep;
+      e.EMermin = e.Etotal - m.ts;
+    }
+    if (n_iter) n_iter[i] = m.n_iter;
+    if (converged) converged[i] = m.conv;
+    if (m.status != 0 && first_bad < 0) {
+      first_bad = i;
+      bad_status = m.status;
+    }
+    if (!m.conv && first_unconv < 0) first_unconv = i;
+  }
+  if (first_bad >= 0) {
+    if (bad_status == kDevIterCap)
+      return set_error(c, DFTBGPU_ERR_ITER_CAP, "batch: molecule %d: eigensolver iteration cap reached", first_bad);
+    if (bad_status == kDevFermiFail)
+      return set_error(c, DFTBGPU_ERR_FERMI, "batch: molecule %d: Fermi level search did not converge", first_bad);
+    return set_error(c, DFTBGPU_ERR_CUDA, "batch: molecule %d: device status %d", first_bad, bad_status);
+  }
+  if (first_unconv >= 0 && o->convergent_only)
+    return set_error(c, DFTBGPU_ERR_SCC_NOT_CONVERGED, "batch: molecule %d: SCC is NOT converged", first_unconv);
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_batch_gradients(dftbgpu_ctx *c, double *grad) {
+  if (!c || !grad) return DFTBGPU_ERR_ARGS;
+  if (!c->batch) return set_error(c, DFTBGPU_ERR_STATE, "batch: no geometries set");
+  cudaSetDevice(c->device);
+  BatchState &b = *c->batch;
+  char msg[256] = {0};
+  const int rc = batch_gradients(c->stream, b, model_view(c), msg, sizeof(msg));
+  if (rc != DFTBGPU_OK) return set_error(c, rc, "%s", msg);
+  DG_CUDA(c, cudaMemcpyAsync(grad, b.d.grad, sizeof(double) * 3 * b.natom, cudaMemcpyDeviceToHost, c->stream));
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
   return DFTBGPU_OK;
 }
 

@@ -132,6 +132,29 @@ int dftbgpu_scc_history(const dftbgpu_ctx *ctx, int cap, double *energy, double 
                         double *ms);
 
 /*
+ * Batched form: many independent molecules (ragged sizes, at most 768 orbitals and 1024 atoms each)
+ * sharing the context's model, solved together. The reference has no batched entry point: its
+ * counterpart is one dftbgpu_set_geometry + dftbgpu_scc (+ dftbgpu_gradients) per molecule, i.e.
+ * one processGeometry call per system (dftbplus/main.F90:1088-1863). Each SCC iteration advances
+ * every unconverged molecule by one iteration (one CTA per molecule, the iteration captured as a
+ * CUDA graph); molecules stop individually once converged.
+ *   set_geometries: atom_off[nmol+1] (atom_off[0] = 0), coords[3*natom] (x,y,z per atom, Bohr,
+ *     molecules concatenated), species[natom] (0-based). DFTBGPU_ERR_NOT_POSDEF names the first
+ *     molecule whose overlap is not positive definite.
+ *   scc: opts as for dftbgpu_scc (net_charge applies to each molecule; DFTBGPU_PREC_MIXED runs FP32
+ *     eigensolves per molecule until its SCC error drops below mixed_switch_tol, then FP64).
+ *     Outputs (each may be NULL): energies[nmol], q_out[natom] (Mulliken populations), n_iter[nmol],
+ *     converged[nmol]. With convergent_only, DFTBGPU_ERR_SCC_NOT_CONVERGED names the first
+ *     unconverged molecule (outputs are still written).
+ *   gradients: grad[3*natom] of the last batched SCC (energy gradients, as dftbgpu_gradients).
+ */
+int dftbgpu_batch_set_geometries(dftbgpu_ctx *ctx, int nmol, const int *atom_off, const double *coords,
+                                 const int *species);
+int dftbgpu_batch_scc(dftbgpu_ctx *ctx, const dftbgpu_scc_opts *opts, dftbgpu_energies *energies,
+                      double *q_out, int *n_iter, int *converged);
+int dftbgpu_batch_gradients(dftbgpu_ctx *ctx, double *grad);
+
+/*
  * Energy gradient (not forces) of the converged state, grad[3*natom] (x,y,z per atom).
  * Energy-weighted density matrix + derivative_blockEuclidean (dftb/forces.F90:548-669, FD SK
  * derivatives nonscc.F90:428-484) + SCC double-counting (scc.F90:794-843) + repulsive
