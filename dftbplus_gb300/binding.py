@@ -58,6 +58,7 @@ SIGNATURES = {
     "dftbgpu_scc_history": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _ip, _dp]),
     "dftbgpu_gradients": (C.c_int, [C.c_void_p, _dp]),
     "dftbgpu_batch_set_geometries": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, _ip]),
+    "dftbgpu_batch_set_geometries_dev": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_void_p, _ip]),
     "dftbgpu_batch_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), C.c_void_p, _dp, _ip, _ip]),
     "dftbgpu_batch_gradients": (C.c_int, [C.c_void_p, _dp]),
     "dftbgpu_gradients_dev": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -231,6 +232,14 @@ class Context:
                                                          _p(xyz, C.c_double), _p(sp, C.c_int)))
         self.batch_atom_off = off
         return off
+
+    def batch_set_geometries_dev(self, atom_off: np.ndarray, coords_dev_ptr: int, species: np.ndarray):
+        """Batched geometries with the (natom, 3) coordinates already on the device."""
+        off = np.ascontiguousarray(atom_off, dtype=np.int32)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        self.check(self.lib.dftbgpu_batch_set_geometries_dev(self.h, len(off) - 1, _p(off, C.c_int),
+                                                             C.c_void_p(coords_dev_ptr), _p(sp, C.c_int)))
+        self.batch_atom_off = off
 
     def batch_scc(self, opts: SccOpts):
         nmol = len(self.batch_atom_off) - 1

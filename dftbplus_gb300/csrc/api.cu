@@ -1033,6 +1033,19 @@ int dftbgpu_batch_set_geometries(dftbgpu_ctx *c, int nmol, const int *atom_off, 
   return DFTBGPU_OK;
 }
 
+int dftbgpu_batch_set_geometries_dev(dftbgpu_ctx *c, int nmol, const int *atom_off, const double *coords_dev,
+                                     const int *species) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (!c->have_model) return set_error(c, DFTBGPU_ERR_STATE, "batch: no model set");
+  cudaSetDevice(c->device);
+  if (!c->batch) c->batch = new BatchState();
+  char msg[256] = {0};
+  const int rc = batch_set_geometries(c->stream, *c->batch, model_view(c), c->h_sp, c->sk_cut_max, nmol, atom_off,
+                                      coords_dev, species, true, msg, sizeof(msg));
+  if (rc != DFTBGPU_OK) return set_error(c, rc, "%s", msg);
+  return DFTBGPU_OK;
+}
+
 int dftbgpu_batch_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, dftbgpu_energies *energies, double *q_out,
                       int *n_iter, int *converged) {
   if (!c || !o) return DFTBGPU_ERR_ARGS;

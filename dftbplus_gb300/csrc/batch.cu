@@ -472,7 +472,7 @@ __device__ int cta_tql(int n, T *d, T *e, T *Z, T *rc, T *rs) {
           bool broke = false;
           for (; i >= l; --i) {
             const T f = s * e[i], b = c * e[i];
-            r = hypot(f, g);
+            r = sqrt(fma(f, f, g * g));   // entries are O(1): no scaling needed
             e[i + 1] = r;
             if (r == T(0)) {
               d[i + 1] -= p;
@@ -480,8 +480,9 @@ __device__ int cta_tql(int n, T *d, T *e, T *Z, T *rc, T *rs) {
               broke = true;
               break;
             }
-            s = f / r;
-            c = g / r;
+            const T ir = T(1) / r;
+            s = f * ir;
+            c = g * ir;
             g = d[i + 1] - p;
             r = (d[i] - g) * s + T(2) * c * b;
             p = s * r;
@@ -503,14 +504,30 @@ __device__ int cta_tql(int n, T *d, T *e, T *Z, T *rc, T *rs) {
       const int lo = s_lo, hi = s_hi;
       if (lo < 0) break;
       if (lo <= hi) {
+        // rows are independent: each thread streams its rows through the rotations, four column
+        // loads in flight ahead of the dependent rotation chain
         for (int k = t; k < n; k += bd) {
-          T carry = Z[k + (size_t)(hi + 1) * n];
-          for (int i = hi; i >= lo; --i) {
-            const T zi = Z[k + (size_t)i * n];
-            Z[k + (size_t)(i + 1) * n] = rs[i] * zi + rc[i] * carry;
-            carry = rc[i] * zi - rs[i] * carry;
+          T *zr = Z + k;
+          T carry = zr[(size_t)(hi + 1) * n];
+          int i = hi;
+          for (; i - 3 >= lo; i -= 4) {
+            const T z0 = zr[(size_t)i * n], z1 = zr[(size_t)(i - 1) * n];
+            const T z2 = zr[(size_t)(i - 2) * n], z3 = zr[(size_t)(i - 3) * n];
+            zr[(size_t)(i + 1) * n] = fma(rs[i], z0, rc[i] * carry);
+            carry = fma(rc[i], z0, -rs[i] * carry);
+            zr[(size_t)i * n] = fma(rs[i - 1], z1, rc[i - 1] * carry);
+            carry = fma(rc[i - 1], z1, -rs[i - 1] * carry);
+            zr[(size_t)(i - 1) * n] = fma(rs[i - 2], z2, rc[i - 2] * carry);
+            carry = fma(rc[i - 2], z2, -rs[i - 2] * carry);
+            zr[(size_t)(i - 2) * n] = fma(rs[i - 3], z3, rc[i - 3] * carry);
+            carry = fma(rc[i - 3], z3, -rs[i - 3] * carry);
           }
-          Z[k + (size_t)lo * n] = carry;
+          for (; i >= lo; --i) {
+            const T zi = zr[(size_t)i * n];
+            zr[(size_t)(i + 1) * n] = fma(rs[i], zi, rc[i] * carry);
+            carry = fma(rc[i], zi, -rs[i] * carry);
+          }
+          zr[(size_t)lo * n] = carry;
         }
       }
       __syncthreads();

@@ -150,6 +150,10 @@ int dftbgpu_scc_history(const dftbgpu_ctx *ctx, int cap, double *energy, double 
  */
 int dftbgpu_batch_set_geometries(dftbgpu_ctx *ctx, int nmol, const int *atom_off, const double *coords,
                                  const int *species);
+/* Same with the coordinates already on the device (coords_dev[3*natom]); atom_off and species on
+ * the host (the orbital layout is host metadata). */
+int dftbgpu_batch_set_geometries_dev(dftbgpu_ctx *ctx, int nmol, const int *atom_off, const double *coords_dev,
+                                     const int *species);
 int dftbgpu_batch_scc(dftbgpu_ctx *ctx, const dftbgpu_scc_opts *opts, dftbgpu_energies *energies,
                       double *q_out, int *n_iter, int *converged);
 int dftbgpu_batch_gradients(dftbgpu_ctx *ctx, double *grad);
