@@ -61,6 +61,7 @@ SIGNATURES = {
     "dftbgpu_batch_set_geometries_dev": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_void_p, _ip]),
     "dftbgpu_batch_scc": (C.c_int, [C.c_void_p, C.POINTER(SccOpts), C.c_void_p, _dp, _ip, _ip]),
     "dftbgpu_batch_gradients": (C.c_int, [C.c_void_p, _dp]),
+    "dftbgpu_grad_params": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "dftbgpu_gradients_dev": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dftbgpu_n_orbitals": (C.c_int, [C.c_void_p, _ip]),
     "dftbgpu_get_orbital_populations": (C.c_int, [C.c_void_p, _dp]),
@@ -136,7 +137,10 @@ class Context:
             pass
 
     def set_model(self, model: Model):
-        p = model.pack()
+        self.set_model_packed(model.pack())
+
+    def set_model_packed(self, p: dict):
+        """Upload a model in the flat layout of Model.pack() (arrays may be replaced, e.g. tables)."""
         self._model_arrays = p  # keep alive
         a = {k: np.ascontiguousarray(v) for k, v in p.items() if isinstance(v, np.ndarray)}
         self.check(self.lib.dftbgpu_set_model(
@@ -176,6 +180,15 @@ class Context:
         g = np.zeros(3 * self.natom)
         self.check(self.lib.dftbgpu_gradients(self.h, _p(g, C.c_double)))
         return g.reshape(self.natom, 3).T.copy()
+
+    def grad_params(self):
+        """dE/d(sk_ham), dE/d(sk_over) (packed table layout) and dE/dU per species."""
+        p = self._model_arrays
+        gh = np.zeros(len(p["sk_ham"]))
+        go = np.zeros(len(p["sk_over"]))
+        gu = np.zeros(p["n_species"])
+        self.check(self.lib.dftbgpu_grad_params(self.h, _p(gh, C.c_double), _p(go, C.c_double), _p(gu, C.c_double)))
+        return gh, go, gu
 
     def orbital_populations(self) -> np.ndarray:
         q = np.zeros(self.norb)

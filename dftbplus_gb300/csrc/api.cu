@@ -28,6 +28,7 @@ struct Ctx {
   double *d_tab = nullptr;
   double *d_rep = nullptr;
   double sk_cut_max = 0.0;
+  long long ham_len = 0;      // table values per kind (H or S), summed over ordered pairs
   bool have_model = false;
   // geometry
   int natom = 0, norb = 0;
@@ -483,6 +484,7 @@ int dftbgpu_set_model(dftbgpu_ctx *c, int nsp, const int *n_shell, const int *an
   long long off = 0, roff = 0;
   long long ham_off = 0;
   for (int p = 0; p < nsp * nsp; ++p) ham_off += (long long)sk_rows[p] * sk_nint[p];
+  c->ham_len = ham_off;
   std::vector<double> tab(2 * (size_t)ham_off);
   std::memcpy(tab.data(), sk_ham, sizeof(double) * ham_off);
   std::memcpy(tab.data() + ham_off, sk_over, sizeof(double) * ham_off);
@@ -857,6 +859,34 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
     DG_CUDA(c, cudaStreamSynchronize(s));
   }
   flush_marks(c);
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_grad_params(dftbgpu_ctx *c, double *dE_dskham, double *dE_dskover, double *dE_dhubbu) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (!c->have_scc) return set_error(c, DFTBGPU_ERR_STATE, "grad_params: call dftbgpu_scc first");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n = c->norb;
+  if (!c->have_w) {
+    energy_weights(s, c->nlevels, c->fill, c->eig, c->fe);
+    DG_CHECK(c, density(c, n, c->nlevels, c->fe, c->W));
+    c->have_w = true;
+  }
+  const size_t nt = (size_t)c->ham_len;
+  double *d = nullptr;
+  DG_CUDA(c, cudaMallocAsync((void **)&d, sizeof(double) * (2 * nt + c->nsp), s));
+  DG_CUDA(c, cudaMemsetAsync(d, 0, sizeof(double) * (2 * nt + c->nsp), s));
+  GeomDev g = geom_view(c);
+  ModelDev m = model_view(c);
+  sk_adjoint(s, m, g, c->d_pi, c->d_pj, c->npairs, c->rho, c->W, c->d_Vout, d, d + nt);
+  hubbard_adjoint(s, m, g, c->d_qout, c->d_q0, d + 2 * nt);
+  DG_CUDA(c, cudaGetLastError());
+  if (dE_dskham) DG_CUDA(c, cudaMemcpyAsync(dE_dskham, d, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
+  if (dE_dskover) DG_CUDA(c, cudaMemcpyAsync(dE_dskover, d + nt, sizeof(double) * nt, cudaMemcpyDeviceToHost, s));
+  if (dE_dhubbu) DG_CUDA(c, cudaMemcpyAsync(dE_dhubbu, d + 2 * nt, sizeof(double) * c->nsp, cudaMemcpyDeviceToHost, s));
+  DG_CUDA(c, cudaFreeAsync(d, s));
+  DG_CUDA(c, cudaStreamSynchronize(s));
   return DFTBGPU_OK;
 }
 

@@ -162,14 +162,10 @@ struct WarpSk {
 };
 
 // Diatomic H and S blocks for species (sp1, sp2) and vector v = R2 - R1 (sk.F90:35-140 layout).
-static __device__ void eval_blocks(const ModelDev &M, int sp1, int sp2, double vx, double vy, double vz,
-                            WarpSk &ws, int lane) {
-  const double dist = sqrt(vx * vx + vy * vy + vz * vz);
-  const double l = vx / dist, m = vy / dist, n = vz / dist;
-  const PairDev &P = M.pair[sp1 * M.nsp + sp2];
-  if (lane < P.n_int) ws.sk[0][lane] = sk_value(P, M.tab, false, lane, dist);
-  if (lane >= 16 && lane - 16 < P.n_int) ws.sk[1][lane - 16] = sk_value(P, M.tab, true, lane - 16, dist);
-  __syncwarp();
+// Rotation of the integrals in ws.sk (H in sk[0], S in sk[1]) into the blocks ws.blk for species
+// (sp1, sp2) and unit vector (l, m, n) from atom 1 to atom 2; linear in ws.sk.
+static __device__ void rotate_blocks(const ModelDev &M, int sp1, int sp2, double l, double m, double n, WarpSk &ws,
+                                     int lane) {
   const SpeciesDev &A = M.sp[sp1];
   const SpeciesDev &B = M.sp[sp2];
   const int npair = A.n_shell * B.n_shell;
@@ -197,6 +193,17 @@ static __device__ void eval_blocks(const ModelDev &M, int sp1, int sp2, double v
     }
   }
   __syncwarp();
+}
+
+static __device__ void eval_blocks(const ModelDev &M, int sp1, int sp2, double vx, double vy, double vz,
+                                   WarpSk &ws, int lane) {
+  const double dist = sqrt(vx * vx + vy * vy + vz * vz);
+  const double l = vx / dist, m = vy / dist, n = vz / dist;
+  const PairDev &P = M.pair[sp1 * M.nsp + sp2];
+  if (lane < P.n_int) ws.sk[0][lane] = sk_value(P, M.tab, false, lane, dist);
+  if (lane >= 16 && lane - 16 < P.n_int) ws.sk[1][lane - 16] = sk_value(P, M.tab, true, lane - 16, dist);
+  __syncwarp();
+  rotate_blocks(M, sp1, sp2, l, m, n, ws, lane);
 }
 
 // ------------------------------------------------------------------------------ short gamma

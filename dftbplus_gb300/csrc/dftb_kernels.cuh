@@ -84,6 +84,12 @@ void gradient_bands(cudaStream_t s, const ModelDev &m, const GeomDev &g, const d
                     const double *W, const double *V, double *grad);
 void gradient_dc_rep(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double *q,
                      const double *q0, double *grad);
+// Parameter adjoints of the converged state (adjoint.cu): dE/d(table values) accumulated into
+// dham/dover (layout of the uploaded sk_ham/sk_over, zeroed by the caller) and dE/dU per species.
+void sk_adjoint(cudaStream_t s, const ModelDev &m, const GeomDev &g, const int *pi, const int *pj, int npairs,
+                const double *rho, const double *W, const double *V, double *dham, double *dover);
+void hubbard_adjoint(cudaStream_t s, const ModelDev &m, const GeomDev &g, const double *q, const double *q0,
+                     double *dU);
 void energy_weights(cudaStream_t s, int k, const double *fill, const double *eig, double *fe);
 
 }  // namespace dg

@@ -167,6 +167,17 @@ int dftbgpu_batch_gradients(dftbgpu_ctx *ctx, double *grad);
 int dftbgpu_gradients(dftbgpu_ctx *ctx, double *grad);
 int dftbgpu_gradients_dev(dftbgpu_ctx *ctx, double *grad_dev);
 
+/*
+ * Gradients of the converged Mermin free energy with respect to the model parameters (the
+ * differentiable form; the reference has no counterpart, its closest relatives being the force
+ * contraction forces.F90:548-669 and the SK interpolation slakoeqgrid.F90:183-244 it differentiates):
+ *   dE_dskham, dE_dskover: same layout and length as sk_ham / sk_over of dftbgpu_set_model (one
+ *     value per grid point, integral and ordered species pair); dE_dhubbu[nsp].
+ * Uses the variational property of the SCC energy (explicit derivatives at fixed rho, W and charges).
+ * Each output may be NULL. Accumulation uses atomics: results are reproducible to rounding only.
+ */
+int dftbgpu_grad_params(dftbgpu_ctx *ctx, double *dE_dskham, double *dE_dskover, double *dE_dhubbu);
+
 /* Sizes and per-orbital Mulliken populations of the converged state (qOutput, mOrb x nAtom
  * collapsed to the nOrb orbitals in atom order). */
 int dftbgpu_n_orbitals(const dftbgpu_ctx *ctx, int *n_orb);
