@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(_HERE, "libdftbgpu.so")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+C_float = C.c_float
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -70,6 +71,10 @@ SIGNATURES = {
     "dftbgpu_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "dftbgpu_test_dgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_double,
                                      _dp, _dp, C.c_double, _dp, C.c_int]),
+    "dftbgpu_set_tensor_cores": (C.c_int, [C.c_int]),
+    "dftbgpu_test_gemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
+                                       C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
+                                       C.POINTER(C.c_float), C.c_int, C.c_int]),
     "dftbgpu_test_tridiag": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_stedc": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
@@ -272,6 +277,19 @@ class Context:
         g = g.reshape(-1, 3).T
         return [g[:, off[i]:off[i + 1]].copy() for i in range(len(off) - 1)]
 
+    def test_gemm_tc(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):
+        """C = alpha op(A) op(B) + beta C on the tensor cores (float32, column-major)."""
+        A = np.asfortranarray(A, dtype=np.float32)
+        B = np.asfortranarray(B, dtype=np.float32)
+        m = A.shape[1] if ta == "T" else A.shape[0]
+        k = A.shape[0] if ta == "T" else A.shape[1]
+        n = B.shape[0] if tb == "T" else B.shape[1]
+        Cm = np.zeros((m, n), dtype=np.float32, order="F") if C is None else np.asfortranarray(C, dtype=np.float32).copy()
+        self.check(self.lib.dftbgpu_test_gemm_tc(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
+                                                 _p(A, C_float), A.shape[0], _p(B, C_float), B.shape[0], beta,
+                                                 _p(Cm, C_float), m, flags))
+        return Cm
+
     def scc_history(self) -> dict:
         """Per-iteration record of the last SCC call: electronic energy, SCC error, precision form
         (PREC_FP64 / PREC_MIXED for an FP32 eigensolve) and host milliseconds."""
@@ -311,6 +329,11 @@ class Context:
 
     def gradients_dev(self, grad_dev_ptr: int):
         self.check(self.lib.dftbgpu_gradients_dev(self.h, C.c_void_p(grad_dev_ptr)))
+
+
+def set_tensor_cores(enable: bool) -> bool:
+    """Route the large FP32 products of the mixed form to the tcgen05 tensor cores (process-wide)."""
+    return bool(load_library().dftbgpu_set_tensor_cores(1 if enable else 0))
 
 
 def default_opts(**kw) -> SccOpts:

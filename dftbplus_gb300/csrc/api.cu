@@ -890,6 +890,36 @@ int dftbgpu_grad_params(dftbgpu_ctx *c, double *dE_dskham, double *dE_dskover, d
   return DFTBGPU_OK;
 }
 
+int dftbgpu_set_tensor_cores(int enable) {
+  const int prev = g_tc_gemm ? 1 : 0;
+  g_tc_gemm = enable != 0;
+  return prev;
+}
+
+int dftbgpu_test_gemm_tc(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, float alpha, const float *a,
+                         int lda, const float *b, int ldb, float beta, float *cm, int ldc, int flags) {
+  if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  const size_t na = (size_t)lda * ((ta == 'N') ? k : m), nb = (size_t)ldb * ((tb == 'N') ? n : k),
+               nc = (size_t)ldc * n;
+  float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  DG_CUDA(c, cudaMalloc((void **)&dA, na * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dB, nb * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dC, nc * sizeof(float)));
+  DG_CUDA(c, cudaMemcpy(dA, a, na * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dB, b, nb * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dC, cm, nc * sizeof(float), cudaMemcpyHostToDevice));
+  const int rc = tc_gemm(c->stream, ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, flags);
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  DG_CUDA(c, cudaMemcpy(cm, dC, nc * sizeof(float), cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  if (rc != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tc_gemm: %s", cudaGetErrorString((cudaError_t)rc));
+  if (tc_gemm_error()) return set_error(c, DFTBGPU_ERR_ITER_CAP, "tc_gemm: a bounded wait timed out");
+  return DFTBGPU_OK;
+}
+
 int dftbgpu_profile_enable(dftbgpu_ctx *c, int enable) {
   if (!c) return DFTBGPU_ERR_ARGS;
   cudaSetDevice(c->device);

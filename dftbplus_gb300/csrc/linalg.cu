@@ -202,7 +202,17 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
   }
   T *P = (splits > 1) ? work : nullptr;
   grid.z = splits;
-  if (!TA && !TB)
+  bool done = false;
+  if constexpr (sizeof(T) == 4) {
+    if (g_tc_gemm && m >= 256 && n >= 256 && k >= 64) {
+      tc_gemm(s, TA ? 'T' : 'N', TB ? 'T' : 'N', m, n, k, (float)alpha, (const float *)A, lda, (const float *)B,
+              ldb, (float)beta, (float *)C, ldc, flags);
+      done = true;
+      P = nullptr;
+    }
+  }
+  if (done) {
+  } else if (!TA && !TB)
     dgemm_kernel<T, false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else if (!TA && TB)
     dgemm_kernel<T, false, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
@@ -210,7 +220,7 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
     dgemm_kernel<T, true, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
   else
     dgemm_kernel<T, true, true><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
-  count_launch();
+  if (!done) count_launch();
   if (P) {
     int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
     dgemm_splitk_reduce<T><<<rb, 256, 0, s>>>(m, n, splits, P, alpha, beta, C, ldc, flags);

@@ -22,6 +22,15 @@ constexpr long long kSplitTarget = 2 * 152;
 template <typename T>
 void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda, const T *B,
           int ldb, T beta, T *C, int ldc, int flags = 0, T *work = nullptr, size_t work_elems = 0);
+// Tensor-core product for FP32 operands (tc_gemm.cu): split-BF16 compensated products on tcgen05
+// with FP32 accumulation in TMEM; same arguments and flags as gemm. Returns a cudaError_t value.
+int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+            const float *B, int ldb, float beta, float *C, int ldc, int flags);
+// Non-zero if a tensor-core GEMM timed out on a bounded wait since the last call (flag cleared).
+int tc_gemm_error();
+// When set, gemm<float> products with m, n >= 256 and k >= 64 use tc_gemm.
+extern bool g_tc_gemm;
+
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
            double *work = nullptr, size_t work_elems = 0);

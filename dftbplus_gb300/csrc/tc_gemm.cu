@@ -1,0 +1,266 @@
+// Tensor-core GEMM for the reduced-precision steps (sm_103a, tcgen05 + TMEM): C = alpha op(A) op(B)
+// + beta C for FP32 operands as split-BF16 compensated products, A B ~ Ah Bh + Ah Bl + Al Bh with
+// Ah = bf16(A), Al = bf16(A - Ah), accumulated in FP32 in tensor memory (relative error ~2^-17).
+//
+// Operands are first packed by a tiled pass into K-major BF16 slabs (hi and lo), padded to whole
+// tiles (128 rows, 64 K) with zeros, with the triangular structure flags applied as masks. The main
+// kernel then streams 128 x 64 tiles of the four slabs into 128-byte-swizzled shared memory (two
+// stages), one elected thread issues 12 tcgen05.mma (3 products x 4 K-steps of 16) per K-block and
+// commits them to an mbarrier, and the epilogue reads the 128 x 128 FP32 tile from TMEM with
+// tcgen05.ld. Every wait is bounded; on a timeout the kernel records an error and releases its TMEM.
+#include <cuda_bf16.h>
+
+#include "linalg.cuh"
+
+namespace dg {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
+constexpr int TC_THREADS = 128;
+constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;               // 16 KB per BF16 tile
+constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;              // Ah, Al, Bh, Bl
+constexpr int TC_SMEM_BYTES = 2 * TC_STAGE_BYTES + 2048;       // two stages + alignment + barriers
+constexpr unsigned kTcSpinLimit = 1u << 26;
+
+// ------------------------------------------------------------------------------ packing
+// Element (r, k) of the packed operand (rows R, K columns) = src[r * rs + k * ks], zero where the
+// mask says the operand is structurally zero (mask 1: keep k <= r, mask 2: keep k >= r), written as
+// hi/lo BF16 pairs at P[r * Kp + k]. 32 x 32 tiles through shared memory, coalesced on both sides.
+__global__ void tc_pack_kernel(int R, int K, const float *src, long long rs, long long ks, int mask, int Kp,
+                               __nv_bfloat16 *Ph, __nv_bfloat16 *Pl) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  const bool k_contig = (ks == 1);
+  for (int q = ty; q < 32; q += 8) {
+    // read: consecutive threads along the contiguous source dimension
+    const int r = k_contig ? r0 + q : r0 + tx;
+    const int k = k_contig ? k0 + tx : k0 + q;
+    float v = 0.f;
+    if (r < R && k < K) {
+      const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
+      if (keep) v = src[(long long)r * rs + (long long)k * ks];
+    }
+    if (k_contig) tile[q][tx] = v;
+    else tile[tx][q] = v;
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int r = r0 + q, k = k0 + tx;
+    const float v = tile[q][tx];
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+    Ph[(size_t)r * Kp + k] = h;
+    Pl[(size_t)r * Kp + k] = l;
+  }
+}
+
+// ------------------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: K-major operand tile, 128-byte swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);   // start address
+  d |= (uint64_t)1 << 16;                     // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset between 8-row groups
+  d |= (uint64_t)1 << 46;                     // descriptor version
+  d |= (uint64_t)2 << 61;                     // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: D FP32, A and B BF16, both K-major, M = 128, N = 128.
+__host__ __device__ constexpr uint32_t tc_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+// Bounded wait for the completion of the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (unsigned it = 0; it < kTcSpinLimit; ++it) {
+    uint32_t ok = 0;
+    asm volatile(
+        "{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, P1;\n\t}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t *v) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// One 128 x 128 tile of C per CTA (128 threads). Packed operands: Ah/Al rows of op(A) (Mp x Kp),
+// Bh/Bl rows of op(B)^T (Np x Kp), K-major BF16.
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, int Kp, const __nv_bfloat16 *Ah,
+                                                              const __nv_bfloat16 *Al, const __nv_bfloat16 *Bh,
+                                                              const __nv_bfloat16 *Bl, float alpha, float beta,
+                                                              float *C, int ldc, int lowerC, int *err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int i0 = blockIdx.x * TC_BM, j0 = blockIdx.y * TC_BN;
+  if (lowerC && j0 > i0 + TC_BM - 1) return;   // whole tile above the diagonal (before any TMEM use)
+  const uint32_t raw = smem_u32(tc_smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  unsigned char *sm = tc_smem_raw + (base - raw);
+  uint64_t *mbars = reinterpret_cast<uint64_t *>(sm + 2 * TC_STAGE_BYTES);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 2 * TC_STAGE_BYTES + 32);
+  if (t == 0) {
+    mbar_init(smem_u32(&mbars[0]), 1);
+    mbar_init(smem_u32(&mbars[1]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"((uint32_t)TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const int nk = Kp / TC_BK;
+  bool ok = true;
+  const __nv_bfloat16 *src[4] = {Ah + (size_t)i0 * Kp, Al + (size_t)i0 * Kp, Bh + (size_t)j0 * Kp,
+                                 Bl + (size_t)j0 * Kp};
+  for (int kb = 0; kb < nk; ++kb) {
+    const int s = kb & 1;
+    unsigned char *stg = sm + s * TC_STAGE_BYTES;
+    if (kb >= 2) {
+      // the MMAs issued two K-blocks ago read this stage
+      if (t == 0 && ok) ok = mbar_wait(smem_u32(&mbars[s]), ((kb - 2) >> 1) & 1);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int mat = 0; mat < 4; ++mat) {
+      const __nv_bfloat16 *g = src[mat] + kb * TC_BK;
+      unsigned char *dst = stg + mat * TC_TILE_BYTES;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int chunk = t + q * TC_THREADS;   // 1024 chunks of 16 bytes per tile
+        const int r = chunk >> 3, c = chunk & 7;
+        const uint4 v = *reinterpret_cast<const uint4 *>(g + (size_t)r * Kp + c * 8);
+        *reinterpret_cast<uint4 *>(dst + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa[2] = {smem_u32(stg), smem_u32(stg + TC_TILE_BYTES)};
+      const uint32_t sb[2] = {smem_u32(stg + 2 * TC_TILE_BYTES), smem_u32(stg + 3 * TC_TILE_BYTES)};
+      const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};   // hi.hi, hi.lo, lo.hi
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 16; ++kk)
+          tc_mma(tmem, tc_sdesc(sa[pa[p]] + kk * 32), tc_sdesc(sb[pb[p]] + kk * 32), tc_idesc(),
+                 (kb | p | kk) != 0 ? 1u : 0u);
+      tc_commit(smem_u32(&mbars[s]));
+    }
+  }
+  if (t == 0 && ok) ok = mbar_wait(smem_u32(&mbars[(nk - 1) & 1]), ((nk - 1) >> 1) & 1);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int row = i0 + warp * 32 + lane;
+#pragma unroll 1
+  for (int cc = 0; cc < TC_BN / 32; ++cc) {
+    uint32_t v[32];
+    tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32), v);
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int col = j0 + cc * 32 + q;
+      if (row < m && col < n && (!lowerC || row >= col)) {
+        float x = alpha * __uint_as_float(v[q]);
+        if (beta != 0.f) x = fmaf(beta, C[row + (size_t)col * ldc], x);
+        C[row + (size_t)col * ldc] = x;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN) : "memory");
+  }
+  if (t == 0 && !ok) atomicExch(err, 1);
+}
+
+// ------------------------------------------------------------------------------ host side
+bool g_tc_gemm = false;   // route large FP32 products through tc_gemm (set by dftbgpu_set_tensor_cores)
+static __nv_bfloat16 *g_tc_ws = nullptr;
+static size_t g_tc_ws_elems = 0;
+static int *g_tc_err = nullptr;
+
+static int round_up(int x, int q) { return (x + q - 1) / q * q; }
+
+int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+            const float *B, int ldb, float beta, float *C, int ldc, int flags) {
+  if (m <= 0 || n <= 0) return 0;
+  const int Mp = round_up(m, TC_BM), Np = round_up(n, TC_BN), Kp = round_up(std::max(k, 1), TC_BK);
+  const size_t need = 2 * ((size_t)Mp + (size_t)Np) * Kp;
+  if (need > g_tc_ws_elems) {
+    cudaDeviceSynchronize();
+    if (g_tc_ws) cudaFree(g_tc_ws);
+    g_tc_ws = nullptr;
+    g_tc_ws_elems = 0;
+    cudaError_t e = cudaMalloc((void **)&g_tc_ws, need * sizeof(__nv_bfloat16));
+    if (e != cudaSuccess) return (int)e;
+    g_tc_ws_elems = need;
+  }
+  if (!g_tc_err) {
+    cudaError_t e = cudaMalloc((void **)&g_tc_err, sizeof(int));
+    if (e != cudaSuccess) return (int)e;
+    cudaMemset(g_tc_err, 0, sizeof(int));
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+      attr = true;
+    }
+  }
+  __nv_bfloat16 *Ah = g_tc_ws, *Al = Ah + (size_t)Mp * Kp, *Bh = Al + (size_t)Mp * Kp, *Bl = Bh + (size_t)Np * Kp;
+  // op(A)(r, k) and op(B)^T(j, k) as strided views; structural zeros from the triangular flags
+  const long long ars = (ta == 'N') ? 1 : lda, aks = (ta == 'N') ? lda : 1;
+  const long long brs = (tb == 'N') ? ldb : 1, bks = (tb == 'N') ? 1 : ldb;
+  const int amask = (flags & kALower) ? 1 : ((flags & kAUpper) ? 2 : 0);
+  const int bmask = (flags & kBLower) ? 2 : ((flags & kBUpper) ? 1 : 0);
+  tc_pack_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, Ah, Al);
+  tc_pack_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, Bh, Bl);
+  tc_gemm_kernel<<<dim3(Mp / TC_BM, Np / TC_BN), TC_THREADS, TC_SMEM_BYTES, s>>>(
+      m, n, Kp, Ah, Al, Bh, Bl, alpha, beta, C, ldc, (flags & kCLower) ? 1 : 0, g_tc_err);
+  count_launch(3);
+  return (int)cudaGetLastError();
+}
+
+int tc_gemm_error() {
+  if (!g_tc_err) return 0;
+  int h = 0;
+  cudaMemcpy(&h, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (h) cudaMemset(g_tc_err, 0, sizeof(int));
+  return h;
+}
+
+}  // namespace dg

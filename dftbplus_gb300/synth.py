@@ -50,8 +50,8 @@ def _draw_h(rng):
     return A, a, b
 
 
-def _draw_s(rng):
-    B = rng.uniform(0.3, 0.9)
+def _draw_s(rng, s_scale=1.0):
+    B = s_scale * rng.uniform(0.3, 0.9)
     c = rng.uniform(0.4, 1.0)
     d = rng.uniform(0.0, 0.3)
     e = rng.uniform(0.0, 0.3)
@@ -101,8 +101,10 @@ def _repulsive(K: float, beta: float, rc: float = REP_CUTOFF, r0: float = 1.0,
                            sp_coeffs=cub, last_coeffs=last)
 
 
-def make_skf_set(species: Sequence[Species], seed: int, draw: int) -> Dict[Tuple[int, int], SkfData]:
-    """Analytic SK tables for all ordered species pairs; ``draw`` selects the sub-stream."""
+def make_skf_set(species: Sequence[Species], seed: int, draw: int,
+                 s_scale: float = 1.0) -> Dict[Tuple[int, int], SkfData]:
+    """Analytic SK tables for all ordered species pairs; ``draw`` selects the sub-stream;
+    ``s_scale`` multiplies the overlap prefactor range B."""
     rng = np.random.default_rng([seed, draw])
     ns = len(species)
     r = GRID_DIST * np.arange(1, GRID_ROWS + 1)
@@ -123,7 +125,7 @@ def make_skf_set(species: Sequence[Species], seed: int, draw: int) -> Dict[Tuple
                     todo.append((l1, l2))
             for (l1, l2) in todo:
                 for m in range(min(l1, l2) + 1):
-                    ph, ps = _draw_h(rng), _draw_s(rng)
+                    ph, ps = _draw_h(rng), _draw_s(rng, s_scale)
                     hv, sv = _h_fun(ph, r), _s_fun(ps, r)
                     if l1 <= l2:
                         col = _COL10[(l1, l2, m)]
@@ -172,9 +174,21 @@ def water_model(seed: int = WATER_SEED, draw: int = WATER_DRAW) -> Model:
     return Model.from_skf(species, make_skf_set(species, seed, draw))
 
 
-def tio2_model(seed: int = WATER_SEED + 1, draw: int = 0) -> Model:
+def tio2_model(seed: int = WATER_SEED + 1, draw: int = 0, s_scale: float = 1.0) -> Model:
     species = [SPECIES_TI, SPECIES_O]
-    return Model.from_skf(species, make_skf_set(species, seed, draw))
+    return Model.from_skf(species, make_skf_set(species, seed, draw, s_scale))
+
+
+# The anatase solid has ~12 neighbours within 3.5 A of every atom; with overlap prefactors drawn from
+# [0.3, 0.9] the overlap is indefinite on it (lambda_min(S) between -1.8 and -4.4 for draws 0-3 on a
+# 200-Ti sphere). The TiO2 workload therefore scales the prefactor range by ANATASE_S_SCALE (every
+# other range as specified) and uses the first draw whose overlap passes the definiteness check.
+ANATASE_S_SCALE = 0.25
+ANATASE_DRAW = 0
+
+
+def anatase_model(draw: int = ANATASE_DRAW) -> Model:
+    return tio2_model(draw=draw, s_scale=ANATASE_S_SCALE)
 
 
 # ---------------------------------------------------------------------------------------- geometry
@@ -214,6 +228,53 @@ def water_cluster(n_mol: int, radius_aa: float, seed: int, min_oo_aa: float = 2.
             coords.append(o + rot @ h)
     coords = np.array(coords).T * AA_BOHR
     species = np.tile(np.array([0, 1, 1], dtype=np.int32), n_mol)
+    return np.ascontiguousarray(coords), species
+
+
+ANATASE_A = 3.785     # A
+ANATASE_C = 9.514     # A
+ANATASE_U = 0.208     # O 8e z parameter
+
+
+def anatase_cluster(n_ti: int = 1700):
+    """(coords[3, N] in Bohr, species[N] with Ti=0, O=1) for a stoichiometric anatase TiO2 sphere.
+
+    Anatase I4_1/amd, a = 3.785 A, c = 9.514 A, Ti on 4a and O on 8e (z = 0.208): per conventional
+    cell Ti at (0,0,0), (0,1/2,1/4), (1/2,1/2,1/2), (1/2,0,3/4) (fractional) and O at each Ti site
+    +- (0, 0, u), so every Ti has two apical O (1.98 A) and four equatorial O (1.93 A). A sphere around a
+    Ti site just large enough for n_ti Ti atoms is carved, then the surplus atoms of the majority
+    species farthest from the centre are removed until Ti:O = 1:2 (ties broken by atom order).
+    Deterministic; there is no random draw.
+    """
+    ti_frac = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.25], [0.5, 0.5, 0.5], [0.5, 0.0, 0.75]])
+    o_frac = []
+    for t in ti_frac:
+        o_frac.append(t + [0.0, 0.0, ANATASE_U])
+        o_frac.append(t - [0.0, 0.0, ANATASE_U])
+    o_frac = np.array(o_frac)
+    dens = 4.0 / (ANATASE_A * ANATASE_A * ANATASE_C)
+    radius = (3.0 * n_ti / (4.0 * math.pi * dens)) ** (1.0 / 3.0) + 2.0
+    na = int(math.ceil(radius / ANATASE_A)) + 1
+    nc = int(math.ceil(radius / ANATASE_C)) + 1
+    cells = np.array([[i, j, k] for i in range(-na, na + 1) for j in range(-na, na + 1) for k in range(-nc, nc + 1)],
+                     dtype=np.float64)
+    scale = np.array([ANATASE_A, ANATASE_A, ANATASE_C])
+    ti = ((cells[:, None, :] + ti_frac[None, :, :]).reshape(-1, 3)) * scale
+    ox = ((cells[:, None, :] + o_frac[None, :, :]).reshape(-1, 3)) * scale
+    rti = np.linalg.norm(ti, axis=1)
+    rox = np.linalg.norm(ox, axis=1)
+    order_ti = np.argsort(rti, kind="stable")[:n_ti]
+    rcut = rti[order_ti[-1]]
+    ti = ti[order_ti]
+    ox = ox[np.argsort(rox, kind="stable")]
+    ox = ox[np.linalg.norm(ox, axis=1) <= rcut + 1e-9]
+    n_o = min(len(ox), 2 * len(ti))
+    ox = ox[:n_o]
+    n_t = n_o // 2
+    ti = ti[:n_t]
+    ox = ox[:2 * n_t]
+    coords = np.concatenate([ti, ox]).T * AA_BOHR
+    species = np.concatenate([np.zeros(len(ti), dtype=np.int32), np.ones(len(ox), dtype=np.int32)])
     return np.ascontiguousarray(coords), species
 
 

@@ -236,6 +236,16 @@ int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *st
  *   tridiag: Householder reduction of the symmetric a (n x n) -> d[n], e[n-1].
  *   stedc:   eigenpairs of the tridiagonal (d, e): d <- eigenvalues ascending, q[n*n] vectors.
  */
+/*
+ * Tensor cores for the reduced-precision products (no reference counterpart): when enabled, FP32
+ * GEMMs of the mixed form with m, n >= 256 run as split-BF16 compensated products on the tcgen05
+ * tensor cores (FP32 accumulation, relative error ~2^-17) instead of FP32 FMA. Process-wide; returns
+ * the previous setting. dftbgpu_test_gemm_tc runs one such product on host arrays (column-major,
+ * flags as the library's triangular GEMM hints) for testing.
+ */
+int dftbgpu_set_tensor_cores(int enable);
+int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha, const float *a,
+                         int lda, const float *b, int ldb, float beta, float *c, int ldc, int flags);
 int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
                        const double *a, const double *b, double beta, double *c, int flags);
 int dftbgpu_test_tridiag(dftbgpu_ctx *ctx, int n, const double *a, double *d, double *e);
