@@ -284,7 +284,7 @@ class Context:
         m = A.shape[1] if ta == "T" else A.shape[0]
         k = A.shape[0] if ta == "T" else A.shape[1]
         n = B.shape[0] if tb == "T" else B.shape[1]
-        Cm = np.zeros((m, n), dtype=np.float32, order="F") if C is None else np.asfortranarray(C, dtype=np.float32).copy()
+        Cm = np.zeros((m, n), dtype=np.float32, order="F") if C is None else np.array(C, dtype=np.float32, order="F")
         self.check(self.lib.dftbgpu_test_gemm_tc(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
                                                  _p(A, C_float), A.shape[0], _p(B, C_float), B.shape[0], beta,
                                                  _p(Cm, C_float), m, flags))
