@@ -664,9 +664,10 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   enum { kFormLow, kFormFull, kFormPert };
   const bool mixed = (o->precision == DFTBGPU_PREC_MIXED);
   int form = mixed ? kFormLow : kFormFull;
-  const double switch_tol = (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 1e-3;
+  const double switch_tol = (o->mixed_switch_tol > 0.0) ? o->mixed_switch_tol : 3e-3;
   constexpr int kMaxPertRun = 16;   // perturbative iterations before the reference is renewed
   int pert_run = 0, k_ref = 0;
+  bool verify = false;   // the next FULL iteration checks a converged perturbative state (k vectors)
   if (mixed) {
     DG_CHECK(c, ensure_mixed(c, n));
     DG_CHECK(c, ensure_pert(c, n, N));
@@ -699,13 +700,22 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       k = k_ref;
       prof_flops(c, kPhPert, 8.0 * nd * nd * (double)k);
       dmpt_scale(s, g, c->d_V, c->Vref, c->C32, c->V32, c->T32, c->Z32);
-      gemm<float>(s, 'T', 'N', n, k, n, 0.5f, c->T32, n, c->V32, n, 0.f, c->Mt32, n);
-      gemm<float>(s, 'T', 'N', n, k, n, 0.5f, c->Z32, n, c->C32, n, 1.f, c->Mt32, n);
+      // FP32 products: tcgen05 split-BF16 tensor cores, or FP32 FMA when they are switched off
+      auto pgemm = [&](char ta, char tb, int mm, int nn, int kk, float al, const float *A, const float *B, float be,
+                       float *Cc, int fl) {
+        if (g_tc_gemm && mm >= 128 && nn >= 128) return tc_gemm(s, ta, tb, mm, nn, kk, al, A, n, B, n, be, Cc, n, fl);
+        gemm<float>(s, ta, tb, mm, nn, kk, al, A, n, B, n, be, Cc, n, fl);
+        return 0;
+      };
+      int grc = 0;
+      grc |= pgemm('T', 'N', n, k, n, 0.5f, c->T32, c->V32, 0.f, c->Mt32, 0);
+      grc |= pgemm('T', 'N', n, k, n, 0.5f, c->Z32, c->C32, 1.f, c->Mt32, 0);
       dmpt_dmu(s, n, k, c->Mt32, c->fill, o->kT, c->d_scal);
       dmpt_response(s, n, k, c->Mt32, c->eig, c->fill, o->kT, c->d_scal);
-      gemm<float>(s, 'N', 'N', n, k, n, 1.f, c->C32, n, c->Mt32, n, 0.f, c->Zp32, n);
-      gemm<float>(s, 'N', 'T', n, n, k, 1.f, c->Zp32, n, c->C32, n, 0.f, c->A32, n, kCLower);
-      gemm<float>(s, 'N', 'T', n, n, k, 1.f, c->C32, n, c->Zp32, n, 1.f, c->A32, n, kCLower);
+      grc |= pgemm('N', 'N', n, k, n, 1.f, c->C32, c->Mt32, 0.f, c->Zp32, 0);
+      grc |= pgemm('N', 'T', n, n, k, 1.f, c->Zp32, c->C32, 0.f, c->A32, kCLower);
+      grc |= pgemm('N', 'T', n, n, k, 1.f, c->C32, c->Zp32, 1.f, c->A32, kCLower);
+      if (grc != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tensor-core GEMM launch failed");
       add_lower_f_sym_d(s, n, c->rho_ref, c->A32, c->rho);
     } else if (form == kFormLow) {
       c->mixed_iters++;
@@ -741,12 +751,13 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       reduced_shift(s, g, c->Lc, c->d_V, c->T);
       dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
       add_half_lower(s, n, c->A0, c->C, c->H);
-      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true, /*all_vectors=*/mixed));
+      const bool reference = mixed && !verify;
+      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true, /*all_vectors=*/reference));
       k = (int)h_scal[kSNLevels];
       mark(c, kPhDensity);
       prof_flops(c, kPhDensity, (double)n * n * k);
       DG_CHECK(c, density(c, n, k, c->fill, c->rho));
-      if (mixed) {
+      if (reference) {
         // reference of the perturbative iterations: C (FP32), X = S C = L Y (FP32), rho, V
         mark(c, kPhPert);
         convert_d2f(s, (size_t)n * n, c->C, c->C32);
@@ -785,13 +796,23 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
         conv = false;
       } else if (form == kFormFull) {
         if (!conv) {
-          form = kFormPert;
-          pert_run = 0;
+          if (verify) {
+            verify = false;   // the check failed: the next FULL iteration becomes a new reference
+          } else {
+            form = kFormPert;
+            pert_run = 0;
+          }
         }
       } else {
         // a converged perturbative state is re-evaluated by a FULL iteration at the same charges
-        // (the mixer leaves q_in unchanged on convergence); so is a long perturbative run
-        if (conv || ++pert_run >= kMaxPertRun) form = kFormFull;
+        // (the mixer leaves q_in unchanged on convergence) that only needs the occupied vectors; a
+        // long perturbative run renews the reference instead
+        if (conv) {
+          form = kFormFull;
+          verify = true;
+        } else if (++pert_run >= kMaxPertRun) {
+          form = kFormFull;
+        }
         conv = false;
       }
     }

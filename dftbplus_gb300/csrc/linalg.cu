@@ -202,15 +202,7 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
   }
   T *P = (splits > 1) ? work : nullptr;
   grid.z = splits;
-  bool done = false;
-  if constexpr (sizeof(T) == 4) {
-    if (g_tc_gemm && m >= 256 && n >= 256 && k >= 64) {
-      tc_gemm(s, TA ? 'T' : 'N', TB ? 'T' : 'N', m, n, k, (float)alpha, (const float *)A, lda, (const float *)B,
-              ldb, (float)beta, (float *)C, ldc, flags);
-      done = true;
-      P = nullptr;
-    }
-  }
+  const bool done = false;
   if (done) {
   } else if (!TA && !TB)
     dgemm_kernel<T, false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);

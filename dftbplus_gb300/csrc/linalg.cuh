@@ -28,7 +28,9 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
             const float *B, int ldb, float beta, float *C, int ldc, int flags);
 // Non-zero if a tensor-core GEMM timed out on a bounded wait since the last call (flag cleared).
 int tc_gemm_error();
-// When set, gemm<float> products with m, n >= 256 and k >= 64 use tc_gemm.
+// When set, the perturbative updates of the mixed form use tc_gemm. Their operands carry the
+// potential change only, so the tensor cores' accumulation (not IEEE round-to-nearest over long K)
+// is scaled down by it; full FP32 eigensolves keep FP32 FMA products.
 extern bool g_tc_gemm;
 
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,

@@ -1,11 +1,14 @@
 // Tensor-core GEMM for the reduced-precision steps (sm_103a, tcgen05 + TMEM): C = alpha op(A) op(B)
-// + beta C for FP32 operands as split-BF16 compensated products, A B ~ Ah Bh + Ah Bl + Al Bh with
-// Ah = bf16(A), Al = bf16(A - Ah), accumulated in FP32 in tensor memory (relative error ~2^-17).
+// + beta C for FP32 operands as split-BF16 compensated products. Each operand is split three ways,
+// A = A0 + A1 + A2 with A0 = bf16(A), A1 = bf16(A - A0), A2 = bf16(A - A0 - A1) (24 significant bits,
+// the FP32 mantissa), and the six leading products A0B0 + A0B1 + A1B0 + A0B2 + A2B0 + A1B1 are
+// accumulated in FP32 in tensor memory (relative error ~2^-22; the three-term form A0B0 + A0B1 +
+// A1B0 keeps only ~17 bits, which stalls the perturbative SCC iterations above 1e-7 e).
 //
-// Operands are first packed by a tiled pass into K-major BF16 slabs (hi and lo), padded to whole
+// Operands are first packed by a tiled pass into K-major BF16 slabs (three per operand), padded to whole
 // tiles (128 rows, 64 K) with zeros, with the triangular structure flags applied as masks. The main
 // kernel then streams 128 x 64 tiles of the four slabs into 128-byte-swizzled shared memory (two
-// stages), one elected thread issues 12 tcgen05.mma (3 products x 4 K-steps of 16) per K-block and
+// stages), one elected thread issues 24 tcgen05.mma (6 products x 4 K-steps of 16) per K-block and
 // commits them to an mbarrier, and the epilogue reads the 128 x 128 FP32 tile from TMEM with
 // tcgen05.ld. Every wait is bounded; on a timeout the kernel records an error and releases its TMEM.
 #include <cuda_bf16.h>
@@ -17,16 +20,18 @@ namespace dg {
 constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
 constexpr int TC_THREADS = 128;
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;               // 16 KB per BF16 tile
-constexpr int TC_STAGE_BYTES = 4 * TC_TILE_BYTES;              // Ah, Al, Bh, Bl
+constexpr int TC_SPLIT = 3;                                    // BF16 pieces per operand
+constexpr int TC_STAGE_BYTES = 2 * TC_SPLIT * TC_TILE_BYTES;   // A0..A2, B0..B2
 constexpr int TC_SMEM_BYTES = 2 * TC_STAGE_BYTES + 2048;       // two stages + alignment + barriers
 constexpr unsigned kTcSpinLimit = 1u << 26;
 
 // ------------------------------------------------------------------------------ packing
 // Element (r, k) of the packed operand (rows R, K columns) = src[r * rs + k * ks], zero where the
 // mask says the operand is structurally zero (mask 1: keep k <= r, mask 2: keep k >= r), written as
-// hi/lo BF16 pairs at P[r * Kp + k]. 32 x 32 tiles through shared memory, coalesced on both sides.
+// three BF16 pieces at P0/P1/P2[r * Kp + k]. 32 x 32 tiles through shared memory, coalesced on both
+// sides.
 __global__ void tc_pack_kernel(int R, int K, const float *src, long long rs, long long ks, int mask, int Kp,
-                               __nv_bfloat16 *Ph, __nv_bfloat16 *Pl) {
+                               __nv_bfloat16 *P0, __nv_bfloat16 *P1, __nv_bfloat16 *P2) {
   __shared__ float tile[32][33];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
@@ -47,10 +52,13 @@ __global__ void tc_pack_kernel(int R, int K, const float *src, long long rs, lon
   for (int q = ty; q < 32; q += 8) {
     const int r = r0 + q, k = k0 + tx;
     const float v = tile[q][tx];
-    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-    Ph[(size_t)r * Kp + k] = h;
-    Pl[(size_t)r * Kp + k] = l;
+    const __nv_bfloat16 b0 = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(b0);
+    const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 b2 = __float2bfloat16_rn(r1 - __bfloat162float(b1));
+    P0[(size_t)r * Kp + k] = b0;
+    P1[(size_t)r * Kp + k] = b1;
+    P2[(size_t)r * Kp + k] = b2;
   }
 }
 
@@ -112,12 +120,12 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t *v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// One 128 x 128 tile of C per CTA (128 threads). Packed operands: Ah/Al rows of op(A) (Mp x Kp),
-// Bh/Bl rows of op(B)^T (Np x Kp), K-major BF16.
-__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, int Kp, const __nv_bfloat16 *Ah,
-                                                              const __nv_bfloat16 *Al, const __nv_bfloat16 *Bh,
-                                                              const __nv_bfloat16 *Bl, float alpha, float beta,
-                                                              float *C, int ldc, int lowerC, int *err) {
+// One 128 x 128 tile of C per CTA (128 threads). Packed operands: PA = three slabs of op(A) rows
+// (each Mp x Kp), PB = three slabs of op(B)^T rows (each Np x Kp), K-major BF16.
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, int Kp, int Mp, int Np,
+                                                              const __nv_bfloat16 *PA, const __nv_bfloat16 *PB,
+                                                              float alpha, float beta, float *C, int ldc, int lowerC,
+                                                              int *err) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int i0 = blockIdx.x * TC_BM, j0 = blockIdx.y * TC_BN;
@@ -144,8 +152,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, in
   const uint32_t tmem = *tslot;
   const int nk = Kp / TC_BK;
   bool ok = true;
-  const __nv_bfloat16 *src[4] = {Ah + (size_t)i0 * Kp, Al + (size_t)i0 * Kp, Bh + (size_t)j0 * Kp,
-                                 Bl + (size_t)j0 * Kp};
+  const __nv_bfloat16 *src[2 * TC_SPLIT];
+#pragma unroll
+  for (int q = 0; q < TC_SPLIT; ++q) {
+    src[q] = PA + (size_t)q * Mp * Kp + (size_t)i0 * Kp;
+    src[TC_SPLIT + q] = PB + (size_t)q * Np * Kp + (size_t)j0 * Kp;
+  }
   for (int kb = 0; kb < nk; ++kb) {
     const int s = kb & 1;
     unsigned char *stg = sm + s * TC_STAGE_BYTES;
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, in
       __syncthreads();
     }
 #pragma unroll
-    for (int mat = 0; mat < 4; ++mat) {
+    for (int mat = 0; mat < 2 * TC_SPLIT; ++mat) {
       const __nv_bfloat16 *g = src[mat] + kb * TC_BK;
       unsigned char *dst = stg + mat * TC_TILE_BYTES;
 #pragma unroll
@@ -170,14 +182,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, in
     __syncthreads();
     if (t == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa[2] = {smem_u32(stg), smem_u32(stg + TC_TILE_BYTES)};
-      const uint32_t sb[2] = {smem_u32(stg + 2 * TC_TILE_BYTES), smem_u32(stg + 3 * TC_TILE_BYTES)};
-      const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};   // hi.hi, hi.lo, lo.hi
+      const uint32_t s0 = smem_u32(stg);
+      // products A0B0, A0B1, A1B0, A0B2, A2B0, A1B1 (largest first)
+      const int pa[6] = {0, 0, 1, 0, 2, 1}, pb[6] = {0, 1, 0, 2, 0, 1};
 #pragma unroll
-      for (int p = 0; p < 3; ++p)
+      for (int p = 0; p < 6; ++p)
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 16; ++kk)
-          tc_mma(tmem, tc_sdesc(sa[pa[p]] + kk * 32), tc_sdesc(sb[pb[p]] + kk * 32), tc_idesc(),
+          tc_mma(tmem, tc_sdesc(s0 + pa[p] * TC_TILE_BYTES + kk * 32),
+                 tc_sdesc(s0 + (TC_SPLIT + pb[p]) * TC_TILE_BYTES + kk * 32), tc_idesc(),
                  (kb | p | kk) != 0 ? 1u : 0u);
       tc_commit(smem_u32(&mbars[s]));
     }
@@ -210,7 +223,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, in
 }
 
 // ------------------------------------------------------------------------------ host side
-bool g_tc_gemm = false;   // route large FP32 products through tc_gemm (set by dftbgpu_set_tensor_cores)
+bool g_tc_gemm = true;    // perturbative updates on the tensor cores (dftbgpu_set_tensor_cores)
 static __nv_bfloat16 *g_tc_ws = nullptr;
 static size_t g_tc_ws_elems = 0;
 static int *g_tc_err = nullptr;
@@ -221,7 +234,7 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
             const float *B, int ldb, float beta, float *C, int ldc, int flags) {
   if (m <= 0 || n <= 0) return 0;
   const int Mp = round_up(m, TC_BM), Np = round_up(n, TC_BN), Kp = round_up(std::max(k, 1), TC_BK);
-  const size_t need = 2 * ((size_t)Mp + (size_t)Np) * Kp;
+  const size_t need = (size_t)TC_SPLIT * ((size_t)Mp + (size_t)Np) * Kp;
   if (need > g_tc_ws_elems) {
     cudaDeviceSynchronize();
     if (g_tc_ws) cudaFree(g_tc_ws);
@@ -241,17 +254,34 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
       attr = true;
     }
   }
-  __nv_bfloat16 *Ah = g_tc_ws, *Al = Ah + (size_t)Mp * Kp, *Bh = Al + (size_t)Mp * Kp, *Bl = Bh + (size_t)Np * Kp;
+  __nv_bfloat16 *PA = g_tc_ws, *PB = PA + (size_t)TC_SPLIT * Mp * Kp;
   // op(A)(r, k) and op(B)^T(j, k) as strided views; structural zeros from the triangular flags
   const long long ars = (ta == 'N') ? 1 : lda, aks = (ta == 'N') ? lda : 1;
   const long long brs = (tb == 'N') ? ldb : 1, bks = (tb == 'N') ? 1 : ldb;
   const int amask = (flags & kALower) ? 1 : ((flags & kAUpper) ? 2 : 0);
   const int bmask = (flags & kBLower) ? 2 : ((flags & kBUpper) ? 1 : 0);
-  tc_pack_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, Ah, Al);
-  tc_pack_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, Bh, Bl);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
+  const bool prof = g_gemm_prof.on && cap == cudaStreamCaptureStatusNone;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (prof) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+  }
+  const size_t sa = (size_t)Mp * Kp, sb = (size_t)Np * Kp;
+  tc_pack_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, PA, PA + sa, PA + 2 * sa);
+  tc_pack_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, PB, PB + sb, PB + 2 * sb);
   tc_gemm_kernel<<<dim3(Mp / TC_BM, Np / TC_BN), TC_THREADS, TC_SMEM_BYTES, s>>>(
-      m, n, Kp, Ah, Al, Bh, Bl, alpha, beta, C, ldc, (flags & kCLower) ? 1 : 0, g_tc_err);
+      m, n, Kp, Mp, Np, PA, PB, alpha, beta, C, ldc, (flags & kCLower) ? 1 : 0, g_tc_err);
   count_launch(3);
+  if (prof) {
+    cudaEventRecord(e1, s);
+    g_gemm_prof.ev.push_back(e0);
+    g_gemm_prof.ev.push_back(e1);
+    g_gemm_prof.flops.push_back(((flags & kCLower) ? 1.0 : 2.0) * m * (double)n * k);
+    g_gemm_prof.fp32.push_back(true);
+  }
   return (int)cudaGetLastError();
 }
 

@@ -60,7 +60,8 @@ typedef struct {
   int precision;          /* DFTBGPU_PREC_* */
   int convergent_only;    /* ConvergentSCCOnly: return DFTBGPU_ERR_SCC_NOT_CONVERGED if 1 */
   double mixed_switch_tol;/* mixed form: leave the FP32 eigensolves once max|q_out - q_in| < this
-                             (0 = default 1e-3); the converged iteration is always FP64 */
+                             (0 = default: 3e-3 single system, 1e-3 batched); the converged
+                             iteration is always FP64 */
 } dftbgpu_scc_opts;
 
 /* Energy terms as in dftb/energytypes.F90 (TEnergies) for this path. */

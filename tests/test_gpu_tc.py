@@ -1,7 +1,8 @@
 """Tensor-core (tcgen05) split-BF16 GEMM against a float64 reference of the same product.
 
-The compensated form Ah Bh + Ah Bl + Al Bh keeps about 17 significant bits, so the bound is
-3e-5 * sum_k |a_ik| |b_kj| per element (plus the FP32 accumulation error)."""
+Three BF16 pieces per operand and the six leading products keep about 22 significant bits; with the
+FP32 accumulation in tensor memory the bound is 2e-6 * sum_k |a_ik| |b_kj| per element (FP32 FMA
+products are within ~1e-6 of the same reference)."""
 import numpy as np
 import pytest
 
@@ -29,7 +30,7 @@ def test_tc_gemm_products(gpu_lib, m, n, k, ta, tb):
     ctx = binding.Context(0)
     C = ctx.test_gemm_tc(ta, tb, A, B)
     ref, mag = _ref(ta, tb, A, B)
-    assert np.all(np.abs(C - ref) <= 3e-5 * mag + 1e-6), np.max(np.abs(C - ref) / (mag + 1e-30))
+    assert np.all(np.abs(C - ref) <= 2e-6 * mag + 1e-6), np.max(np.abs(C - ref) / (mag + 1e-30))
     ctx.close()
 
 
@@ -48,6 +49,6 @@ def test_tc_gemm_flags_and_beta(gpu_lib):
     ref = 0.5 * L.astype(np.float64) @ X + C0
     mag = 0.5 * np.abs(L).astype(np.float64) @ np.abs(X) + np.abs(C0)
     low = np.tril(np.ones((n, n), dtype=bool))
-    assert np.all(np.abs(C - ref)[low] <= 3e-5 * mag[low] + 1e-6)
+    assert np.all(np.abs(C - ref)[low] <= 2e-6 * mag[low] + 1e-6)
     assert np.array_equal(C[~low], C0[~low])       # upper triangle untouched
     ctx.close()
