@@ -842,79 +842,21 @@ __global__ void batch_scc_init_kernel(BatchDev B, BatchOpts o) {
     st.form = o.mixed ? 1 : 0;
     st.err = 0.0;
     st.k = 0;
+    st.verify = 0;
+    st.pert_run = 0;
   }
 }
 
-// One SCC iteration of every eligible molecule (one CTA each): V = gamma dq_in, reduced
-// A = A0 + 1/2 (B + B^T) with B = L^-1 diag(V) L, eigen-decomposition (Householder + implicit QL in
-// precision T), Fermi filling, C = L^-T Y, rho = C f C^T, Mulliken populations, E_nonSCC, E_SCC and
-// the molecule's Broyden step. FP32 molecules (mixed form) move to FP64 once their SCC error drops
-// below switch_tol (the converged iteration is always FP64); the last allowed iteration is FP64.
-// Molecules still active afterwards are counted in *active.
-template <typename T>
-__global__ void __launch_bounds__(kBatchThreads) batch_iter_kernel(ModelDev M, BatchDev B, BatchOpts o, int *active) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ T As[GT][GT + 1], Bs[GT][GT + 1];
-  __shared__ double sh_s[33], sh_c[33];
-  __shared__ T shT[33];
-  __shared__ int sh_i;
+// Common end of an SCC iteration of one molecule: Mulliken populations and Tr(rho H0)
+// (populations.F90:120-191, getenergies.F90:198-199), output potentials, E_SCC and the molecule's
+// Broyden step; thread 0 records the iteration in st. Returns the convergence flag (all threads).
+__device__ bool cta_iter_tail(const BatchDev &B, const BatchOpts &o, const MolV &mv, int id, int it,
+                              const double *rho, double *sh_s, double *sh_c) {
   const int t = threadIdx.x, bd = blockDim.x, lane = t & 31, warp = t >> 5, nw = bd >> 5;
-  const int id = B.order[blockIdx.x];
+  const int n = mv.n, nat = mv.nat;
   MolState &st = B.st[id];
-  const bool is32 = sizeof(T) == 4;
-  const int nit = st.n_iter;
-  bool elig = st.status == 0 && !st.conv && nit < o.max_iter;
-  if (is32) elig = elig && st.form == 1 && nit + 1 < o.max_iter;
-  else elig = elig && (st.form == 0 || nit + 1 == o.max_iter);
-  if (!elig) return;
-  const MolV mv = mol_view(B, id);
-  const int n = mv.n, nat = mv.nat, it = nit + 1;
-  T *L, *Li, *A0, *A, *Tm, *Z;
-  mats(B, mv.mo, &L, &Li, &A0, &A, &Tm, &Z);
-  double *qin = B.qin + mv.a0, *qout = B.qout + mv.a0, *V = B.V + mv.a0, *Vout = B.Vout + mv.a0;
+  double *qin = B.qin + mv.a0, *qout = B.qout + mv.a0, *Vout = B.Vout + mv.a0;
   const double *q0 = B.q0 + mv.a0, *gam = B.gam + mv.go;
-  T *sv = reinterpret_cast<T *>(dsm), *sw = sv + n, *sd = sw + n, *se = sd + n;
-  int *perm = reinterpret_cast<int *>(se + n);
-  const size_t nn = (size_t)n * n;
-  // potentials of the input charges
-  for (int a = t; a < nat; a += bd) {
-    double s = 0.0;
-    for (int b = 0; b < nat; ++b) s = fma(gam[a + (size_t)b * nat], qin[b] - q0[b], s);
-    V[a] = s;
-  }
-  __syncthreads();
-  for (size_t idx = t; idx < nn; idx += bd) {
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    Tm[idx] = (i >= j) ? (T)V[B.o_atom[mv.o0 + i] - mv.a0] * L[idx] : T(0);
-  }
-  __syncthreads();
-  cta_gemm<T, T>(n, n, n, T(1), Li, n, false, Tm, n, false, T(0), Z, n, kGLowerC | kGALower | kGBLower, As, Bs);
-  for (size_t idx = t; idx < nn; idx += bd) {
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    const T bij = Z[max(i, j) + (size_t)min(i, j) * n];
-    A[idx] = A0[idx] + ((i == j) ? bij : T(0.5) * bij);
-  }
-  __syncthreads();
-  cta_tridiag<T>(n, A, Z, sd, se, sv, sw, shT);
-  const int qs = cta_tql<T>(n, sd, se, Z, sv, sw);
-  double *eig = B.eig + mv.o0, *fill = B.fill + mv.o0;
-  cta_sort_eig<T>(n, sd, Z, eig, Tm, perm);
-  const int fs = cta_fermi(n, eig, st.nel, o.kT, fill, st, sh_s, sh_c, &sh_i);
-  const int k = st.k;
-  double *rho = B.rho + mv.mo;
-  if (k > 0) {
-    cta_gemm<T, T>(n, k, n, T(1), Li, n, true, Tm, n, false, T(0), Z, n, kGAUpper, As, Bs);
-    for (size_t idx = t; idx < (size_t)n * k; idx += bd) A[idx] = Z[idx] * (T)fill[idx / n];
-    __syncthreads();
-    cta_gemm<T, double>(n, n, k, T(1), A, n, false, Z, n, true, T(0), rho, n, kGLowerC, As, Bs);
-    for (size_t idx = t; idx < nn; idx += bd) {
-      const int i = (int)(idx % n), j = (int)(idx / n);
-      if (i < j) rho[idx] = rho[j + (size_t)i * n];
-    }
-  } else {
-    for (size_t idx = t; idx < nn; idx += bd) rho[idx] = 0.0;
-  }
-  __syncthreads();
   // Mulliken (populations.F90:120-191) and Tr(rho H0) (getenergies.F90:198-199)
   double *qo = B.dd + mv.o0, *eo = B.ee + mv.o0;
   const double *S = B.S + mv.mo, *H0 = B.H0 + mv.mo;
@@ -959,21 +901,231 @@ __global__ void __launch_bounds__(kBatchThreads) batch_iter_kernel(ModelDev M, B
   bool conv = false;
   const double err = cta_broyden(nat, it, st.mix_calls + 1, o.min_iter, o.max_iter, o.tol, o, bm, qin, qout, &conv,
                                  sh_s);
+  __shared__ int s_conv;
   if (t == 0) {
     st.n_iter = it;
     st.err = err;
     st.enonscc = enonscc;
     st.escc = escc;
     if (!conv && it != o.max_iter) st.mix_calls += 1;
+    s_conv = conv ? 1 : 0;
+  }
+  __syncthreads();
+  return s_conv != 0;
+}
+
+// One SCC iteration of every eligible molecule (one CTA each): V = gamma dq_in, reduced
+// A = A0 + 1/2 (B + B^T) with B = L^-1 diag(V) L, eigen-decomposition (Householder + implicit QL in
+// precision T), Fermi filling, C = L^-T Y, rho = C f C^T, Mulliken populations, E_nonSCC, E_SCC and
+// the molecule's Broyden step. FP32 molecules (mixed form) move to FP64 once their SCC error drops
+// below switch_tol (the converged iteration is always FP64); the last allowed iteration is FP64.
+// Molecules still active afterwards are counted in *active.
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads) batch_iter_kernel(ModelDev M, BatchDev B, BatchOpts o, int *active) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ T As[GT][GT + 1], Bs[GT][GT + 1];
+  __shared__ double sh_s[33], sh_c[33];
+  __shared__ T shT[33];
+  __shared__ int sh_i;
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int id = B.order[blockIdx.x];
+  MolState &st = B.st[id];
+  const bool is32 = sizeof(T) == 4;
+  const int nit = st.n_iter;
+  bool elig = st.status == 0 && !st.conv && nit < o.max_iter;
+  if (is32) elig = elig && st.form == 1 && nit + 1 < o.max_iter;
+  else elig = elig && (st.form == 0 || nit + 1 == o.max_iter);
+  if (!elig) return;
+  const MolV mv = mol_view(B, id);
+  const int n = mv.n, nat = mv.nat, it = nit + 1;
+  T *L, *Li, *A0, *A, *Tm, *Z;
+  mats(B, mv.mo, &L, &Li, &A0, &A, &Tm, &Z);
+  double *qin = B.qin + mv.a0, *V = B.V + mv.a0;
+  const double *q0 = B.q0 + mv.a0, *gam = B.gam + mv.go;
+  T *sv = reinterpret_cast<T *>(dsm), *sw = sv + n, *sd = sw + n, *se = sd + n;
+  int *perm = reinterpret_cast<int *>(se + n);
+  const size_t nn = (size_t)n * n;
+  // potentials of the input charges
+  for (int a = t; a < nat; a += bd) {
+    double s = 0.0;
+    for (int b = 0; b < nat; ++b) s = fma(gam[a + (size_t)b * nat], qin[b] - q0[b], s);
+    V[a] = s;
+  }
+  __syncthreads();
+  for (size_t idx = t; idx < nn; idx += bd) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    Tm[idx] = (i >= j) ? (T)V[B.o_atom[mv.o0 + i] - mv.a0] * L[idx] : T(0);
+  }
+  __syncthreads();
+  cta_gemm<T, T>(n, n, n, T(1), Li, n, false, Tm, n, false, T(0), Z, n, kGLowerC | kGALower | kGBLower, As, Bs);
+  for (size_t idx = t; idx < nn; idx += bd) {
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    const T bij = Z[max(i, j) + (size_t)min(i, j) * n];
+    A[idx] = A0[idx] + ((i == j) ? bij : T(0.5) * bij);
+  }
+  __syncthreads();
+  cta_tridiag<T>(n, A, Z, sd, se, sv, sw, shT);
+  const int qs = cta_tql<T>(n, sd, se, Z, sv, sw);
+  double *eig = B.eig + mv.o0, *fill = B.fill + mv.o0;
+  cta_sort_eig<T>(n, sd, Z, eig, Tm, perm);
+  const int fs = cta_fermi(n, eig, st.nel, o.kT, fill, st, sh_s, sh_c, &sh_i);
+  const int k = st.k;
+  double *rho = B.rho + mv.mo;
+  // an FP64 iteration of the mixed form that is not a check of a perturbative state becomes the
+  // reference of the perturbative updates: it keeps all n vectors
+  const bool reference = !is32 && o.mixed && !st.verify;
+  const int kc = reference ? n : k;
+  if (kc > 0 && kc != k)
+    cta_gemm<T, T>(n, kc, n, T(1), Li, n, true, Tm, n, false, T(0), Z, n, kGAUpper, As, Bs);
+  if (k > 0) {
+    if (kc == k) cta_gemm<T, T>(n, k, n, T(1), Li, n, true, Tm, n, false, T(0), Z, n, kGAUpper, As, Bs);
+    for (size_t idx = t; idx < (size_t)n * k; idx += bd) A[idx] = Z[idx] * (T)fill[idx / n];
+    __syncthreads();
+    cta_gemm<T, double>(n, n, k, T(1), A, n, false, Z, n, true, T(0), rho, n, kGLowerC, As, Bs);
+    for (size_t idx = t; idx < nn; idx += bd) {
+      const int i = (int)(idx % n), j = (int)(idx / n);
+      if (i < j) rho[idx] = rho[j + (size_t)i * n];
+    }
+  } else {
+    for (size_t idx = t; idx < nn; idx += bd) rho[idx] = 0.0;
+  }
+  __syncthreads();
+  if constexpr (sizeof(T) == 8) {
+    if (reference) {
+      // X = S C = L Y (Y: the sorted eigenvectors in Tm), FP32 copies of C and X, rho_ref, V_ref
+      cta_gemm<T, T>(n, n, n, T(1), L, n, false, Tm, n, false, T(0), A, n, kGALower, As, Bs);
+      float *X32 = B.X32 + mv.mo, *C32 = B.C32 + mv.mo;
+      double *rref = B.rho_ref + mv.mo;
+      for (size_t idx = t; idx < nn; idx += bd) {
+        X32[idx] = (float)A[idx];
+        C32[idx] = (float)Z[idx];
+        rref[idx] = rho[idx];
+      }
+      for (int a = t; a < nat; a += bd) B.Vref[mv.a0 + a] = V[a];
+      __syncthreads();
+    }
+  }
+  const bool conv = cta_iter_tail(B, o, mv, id, it, rho, sh_s, sh_c);
+  if (t == 0) {
     const int status = qs ? qs : fs;
     if (status) st.status = status;
     bool c = conv;
-    if (is32 && (conv || err < o.switch_tol)) {
-      st.form = 0;   // re-evaluated in FP64, never accepted in FP32
-      c = false;
+    if (is32) {
+      if (conv || st.err < o.switch_tol) {
+        st.form = 0;   // re-evaluated in FP64, never accepted in FP32
+        c = false;
+      }
+    } else if (o.mixed && !c) {
+      if (st.verify) {
+        st.verify = 0;   // the check failed: the next FP64 iteration becomes a new reference
+      } else if (reference) {
+        st.form = 2;
+        st.pert_run = 0;
+      }
     }
     st.conv = c ? 1 : 0;
     if (!c && st.status == 0 && it < o.max_iter) atomicAdd(active, 1);
+  }
+}
+
+
+// Perturbative SCC iteration of the mixed form for every molecule in that state (one CTA each):
+// first-order density-matrix perturbation around the molecule's last FP64 reference (the same
+// scheme as the single-system form): D = diag(V - V_ref), M = 1/2 (X^T D C + C^T D X) for the k
+// occupied columns, dP_ij = K_ij (M_ij - dmu delta_ij) with the Fermi divided differences K,
+// rho = rho_ref + C dP C^T, in FP32 per-CTA products (the operands carry the potential change only).
+// A converged state is checked by an FP64 iteration with the occupied vectors; 16 perturbative
+// iterations without convergence renew the reference.
+constexpr int kBatchMaxPertRun = 16;
+__global__ void __launch_bounds__(kBatchThreads) batch_pert_kernel(ModelDev M, BatchDev B, BatchOpts o, int *active) {
+  __shared__ float As[GT][GT + 1], Bs[GT][GT + 1];
+  __shared__ double sh_s[33], sh_c[33], s_dmu;
+  const int t = threadIdx.x, bd = blockDim.x;
+  const int id = B.order[blockIdx.x];
+  MolState &st = B.st[id];
+  const int nit = st.n_iter;
+  if (!(st.status == 0 && !st.conv && st.form == 2 && nit + 1 < o.max_iter)) return;
+  const MolV mv = mol_view(B, id);
+  const int n = mv.n, nat = mv.nat, it = nit + 1, k = st.k;
+  const size_t nn = (size_t)n * n;
+  const double *qin = B.qin + mv.a0, *q0 = B.q0 + mv.a0, *gam = B.gam + mv.go, *Vref = B.Vref + mv.a0;
+  double *V = B.V + mv.a0;
+  const float *X = B.X32 + mv.mo, *Cf = B.C32 + mv.mo;
+  float *DC = B.A32 + mv.mo, *DX = B.T32 + mv.mo, *Mt = B.Mt32 + mv.mo, *Zp = B.Zp32 + mv.mo, *D = B.Z32 + mv.mo;
+  const double *eig = B.eig + mv.o0, *fill = B.fill + mv.o0, *rref = B.rho_ref + mv.mo;
+  double *rho = B.rho + mv.mo;
+  for (int a = t; a < nat; a += bd) {
+    double s = 0.0;
+    for (int b = 0; b < nat; ++b) s = fma(gam[a + (size_t)b * nat], qin[b] - q0[b], s);
+    V[a] = s;
+  }
+  __syncthreads();
+  for (size_t idx = t; idx < nn; idx += bd) {
+    const int l = (int)(idx % n);
+    const int a = B.o_atom[mv.o0 + l] - mv.a0;
+    const float dv = (float)(V[a] - Vref[a]);
+    DC[idx] = dv * Cf[idx];
+    DX[idx] = dv * X[idx];
+  }
+  __syncthreads();
+  if (k > 0) {
+    cta_gemm<float, float>(n, k, n, 0.5f, DC, n, true, X, n, false, 0.f, Mt, n, 0, As, Bs);
+    cta_gemm<float, float>(n, k, n, 0.5f, DX, n, true, Cf, n, false, 1.f, Mt, n, 0, As, Bs);
+    // Fermi-level shift from charge conservation
+    double num = 0.0, den = 0.0;
+    for (int i = t; i < k; i += bd) {
+      const double f = fill[i];
+      const double fp = -f * (2.0 - f) / (2.0 * o.kT);
+      num = fma(fp, (double)Mt[i + (size_t)i * n], num);
+      den += fp;
+    }
+    num = cta_sum(num, sh_s);
+    den = cta_sum(den, sh_c);
+    if (t == 0) s_dmu = (fabs(den) > 1e-300) ? num / den : 0.0;
+    __syncthreads();
+    const double dmu = s_dmu;
+    for (size_t idx = t; idx < (size_t)n * k; idx += bd) {
+      const int j = (int)(idx % n), i = (int)(idx / n);
+      const double fi = fill[i];
+      double mij = (double)Mt[idx], K;
+      if (j == i) {
+        K = -fi * (2.0 - fi) / (2.0 * o.kT);
+        mij -= dmu;
+      } else {
+        const double de = eig[i] - eig[j];
+        if (fabs(de) > 1e-9) {
+          K = (fi - fill[j]) / de;
+        } else {
+          const double fm = 0.5 * (fi + fill[j]);
+          K = -fm * (2.0 - fm) / (2.0 * o.kT);
+        }
+      }
+      double v = K * mij;
+      if (j < k) v *= 0.5;
+      Mt[idx] = (float)v;
+    }
+    __syncthreads();
+    cta_gemm<float, float>(n, k, n, 1.f, Cf, n, false, Mt, n, false, 0.f, Zp, n, 0, As, Bs);
+    cta_gemm<float, float>(n, n, k, 1.f, Zp, n, false, Cf, n, true, 0.f, D, n, kGLowerC, As, Bs);
+    cta_gemm<float, float>(n, n, k, 1.f, Cf, n, false, Zp, n, true, 1.f, D, n, kGLowerC, As, Bs);
+    for (size_t idx = t; idx < nn; idx += bd) {
+      const int i = (int)(idx % n), j = (int)(idx / n);
+      rho[idx] = rref[idx] + (double)((i >= j) ? D[idx] : D[j + (size_t)i * n]);
+    }
+  } else {
+    for (size_t idx = t; idx < nn; idx += bd) rho[idx] = rref[idx];
+  }
+  __syncthreads();
+  const bool conv = cta_iter_tail(B, o, mv, id, it, rho, sh_s, sh_c);
+  if (t == 0) {
+    if (conv) {
+      st.form = 0;     // checked by an FP64 iteration at the same charges
+      st.verify = 1;
+    } else if (++st.pert_run >= kBatchMaxPertRun) {
+      st.form = 0;     // renew the reference
+    }
+    st.conv = 0;
+    if (st.status == 0 && it < o.max_iter) atomicAdd(active, 1);
   }
 }
 
@@ -1203,7 +1355,10 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     e |= balloc(b, &d.grad, 3 * NA, b.owned);
     for (double **pp : {&d.eig, &d.fill, &d.dd, &d.ee}) e |= balloc(b, pp, NO, b.owned);
     for (double **pp : {&d.H0, &d.S, &d.L, &d.Li, &d.A0, &d.A, &d.T, &d.Z, &d.rho}) e |= balloc(b, pp, MM, b.owned);
-    for (float **pp : {&d.L32, &d.Li32, &d.A0_32, &d.A32, &d.T32, &d.Z32}) e |= balloc(b, pp, MM, b.owned);
+    for (float **pp : {&d.L32, &d.Li32, &d.A0_32, &d.A32, &d.T32, &d.Z32, &d.X32, &d.C32, &d.Mt32, &d.Zp32})
+      e |= balloc(b, pp, MM, b.owned);
+    e |= balloc(b, &d.rho_ref, MM, b.owned);
+    e |= balloc(b, &d.Vref, NA, b.owned);
     e |= balloc(b, &d.gam, NG, b.owned);
     e |= balloc(b, &d.st, NM, b.owned);
     e |= balloc(b, &b.d_active, 1, b.owned);
@@ -1297,7 +1452,10 @@ int batch_scc(cudaStream_t s, BatchState &b, const ModelDev &m, const BatchOpts 
   if (ce == cudaSuccess) {
     cudaMemsetAsync(b.d_active, 0, sizeof(int), s);
     batch_iter_kernel<double><<<b.nmol, kBatchThreads, sm64, s>>>(m, d, o, b.d_active);
-    if (o.mixed) batch_iter_kernel<float><<<b.nmol, kBatchThreads, sm32, s>>>(m, d, o, b.d_active);
+    if (o.mixed) {
+      batch_iter_kernel<float><<<b.nmol, kBatchThreads, sm32, s>>>(m, d, o, b.d_active);
+      batch_pert_kernel<<<b.nmol, kBatchThreads, 0, s>>>(m, d, o, b.d_active);
+    }
     cudaMemcpyAsync(b.h_active, b.d_active, sizeof(int), cudaMemcpyDeviceToHost, s);
     ce = cudaStreamEndCapture(s, &g);
   }
@@ -1311,7 +1469,7 @@ int batch_scc(cudaStream_t s, BatchState &b, const ModelDev &m, const BatchOpts 
     ce = cudaGraphLaunch(b.graph, s);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
     if (ce != cudaSuccess) return fail(msg, len, DFTBGPU_ERR_CUDA, cudaGetErrorString(ce));
-    count_launch(o.mixed ? 2 : 1);
+    count_launch(o.mixed ? 3 : 1);
     if (*b.h_active == 0) break;
   }
   b.have_scc = true;

@@ -18,8 +18,10 @@ struct MolState {
   int n_iter;      // SCC iterations done
   int mix_calls;   // Broyden mixing steps taken
   int conv;        // converged (FP64 iteration)
-  int form;        // 0: FP64 eigensolves, 1: FP32 eigensolves (mixed form, early iterations)
+  int form;        // 0: FP64 eigensolve, 1: FP32 eigensolve, 2: perturbative update (mixed form)
   int status;      // DevStatus of the molecule (non-zero: failed, no further iterations)
+  int verify;      // the next FP64 iteration checks a converged perturbative state (occupied vectors)
+  int pert_run;    // perturbative iterations since the last reference
 };
 
 struct BatchDev {
@@ -36,6 +38,10 @@ struct BatchDev {
   // per-molecule matrices (column-major, leading dimension n of the molecule)
   double *H0, *S, *L, *Li, *A0, *A, *T, *Z, *rho;
   float *L32, *Li32, *A0_32, *A32, *T32, *Z32;
+  // perturbative updates of the mixed form: reference C (all vectors) and X = S C in FP32, Mt / C dP
+  // work arrays, reference density (FP64) and reference potentials (per atom)
+  float *X32, *C32, *Mt32, *Zp32;
+  double *rho_ref, *Vref;
   double *gam;                      // gamma matrix (1/r - short gamma, U on the diagonal)
   // per-orbital vectors
   double *eig, *fill, *dd, *ee;
