@@ -1158,12 +1158,70 @@ __global__ void __launch_bounds__(kBatchThreads) batch_ew_kernel(BatchDev B) {
   }
 }
 
-// Gradient of every atom: band term with central-difference SK block derivatives
-// (forces.F90:548-669, nonscc.F90:428-484, delta = 2^-13), SCC double counting
-// (shortgamma.F90:349-411, coulomb.F90:1140-1185) and repulsive (twobodyrep.F90:273-332), partners
-// restricted to the atom's molecule. One warp per atom, each pair evaluated from both sides.
+// Band term of the gradient per atom pair (i < j) of each molecule: central-difference SK block
+// derivatives (forces.F90:548-669, nonscc.F90:428-484, delta = 2^-13) contracted with rho, W and the
+// potential shift; the contribution to atom i is stored (atom j receives its negative). One CTA of
+// four warps per molecule, one warp per pair; every pair is evaluated once.
+__global__ void __launch_bounds__(128) batch_pair_grad_kernel(ModelDev M, BatchDev B) {
+  __shared__ WarpSk ws_all[4][6];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int id = B.order[blockIdx.x];
+  if (B.st[id].status != 0) return;
+  const MolV mv = mol_view(B, id);
+  const int n = mv.n, nat = mv.nat;
+  const double *rho = B.rho + mv.mo, *W = B.A + mv.mo, *Vo = B.Vout + mv.a0;
+  double *dp = B.dpair + 3 * B.pair_off[id];
+  const double delta = 1.220703125e-4;
+  const double inv2d = 1.0 / (2.0 * delta);
+  for (int l1 = 0; l1 < nat; ++l1) {
+    for (int l2 = l1 + 1 + w; l2 < nat; l2 += 4) {
+      const long long p = (long long)l1 * (2 * nat - l1 - 1) / 2 + (l2 - l1 - 1);
+      const int a1 = mv.a0 + l1, a2 = mv.a0 + l2;
+      const int s1 = B.species[a1], s2 = B.species[a2];
+      const double bx = B.xyz[3 * a2] - B.xyz[3 * a1];
+      const double by = B.xyz[3 * a2 + 1] - B.xyz[3 * a1 + 1];
+      const double bz = B.xyz[3 * a2 + 2] - B.xyz[3 * a1 + 2];
+      const PairDev &P = M.pair[s1 * M.nsp + s2];
+      if (bx * bx + by * by + bz * bz > P.sk_cut * P.sk_cut) {
+        if (lane < 3) dp[3 * p + lane] = 0.0;
+        continue;
+      }
+      for (int kq = 0; kq < 3; ++kq)
+        for (int ii = 0; ii < 2; ++ii) {
+          double v[3] = {bx, by, bz};
+          v[kq] -= (double)(2 * (ii + 1) - 3) * delta;
+          eval_blocks(M, s1, s2, v[0], v[1], v[2], ws_all[w][kq * 2 + ii], lane);
+        }
+      const int o1 = B.a_orb[a1] - mv.o0, o2 = B.a_orb[a2] - mv.o0;
+      const int n1 = M.sp[s1].n_orb, n2 = M.sp[s2].n_orb;
+      const double vs = 0.5 * (Vo[l1] + Vo[l2]);
+      double dt[3] = {0.0, 0.0, 0.0};
+      for (int idx = lane; idx < n1 * n2; idx += 32) {
+        const int bb = idx % n2, aa = idx / n2;
+        const double rv = rho[(o2 + bb) + (size_t)(o1 + aa) * n];
+        const double wv = W[(o2 + bb) + (size_t)(o1 + aa) * n];
+#pragma unroll
+        for (int kq = 0; kq < 3; ++kq) {
+          const double dh = (ws_all[w][2 * kq + 1].blk[0][bb][aa] - ws_all[w][2 * kq].blk[0][bb][aa]) * inv2d;
+          const double ds = (ws_all[w][2 * kq + 1].blk[1][bb][aa] - ws_all[w][2 * kq].blk[1][bb][aa]) * inv2d;
+          dt[kq] += 2.0 * (rv * dh - wv * ds) + 2.0 * vs * ds * rv;
+        }
+      }
+      const double gx = warp_sum(dt[0]), gy = warp_sum(dt[1]), gz = warp_sum(dt[2]);
+      if (lane == 0) {
+        dp[3 * p] = gx;
+        dp[3 * p + 1] = gy;
+        dp[3 * p + 2] = gz;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Gradient of every atom: the band terms of its pairs (summed in partner order, deterministic),
+// SCC double counting (shortgamma.F90:349-411, coulomb.F90:1140-1185) and repulsive
+// (twobodyrep.F90:273-332), partners restricted to the atom's molecule. One warp per atom.
 __global__ void __launch_bounds__(64) batch_grad_kernel(ModelDev M, BatchDev B) {
-  __shared__ WarpSk ws_all[2][6];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gA = blockIdx.x * 2 + w;
   if (gA >= B.natom) return;
@@ -1173,47 +1231,19 @@ __global__ void __launch_bounds__(64) batch_grad_kernel(ModelDev M, BatchDev B) 
     return;
   }
   const MolV mv = mol_view(B, id);
-  const int n = mv.n, a = gA - mv.a0;
-  const double *rho = B.rho + mv.mo, *W = B.A + mv.mo, *Vo = B.Vout + mv.a0;
-  const double delta = 1.220703125e-4;
-  const double inv2d = 1.0 / (2.0 * delta);
+  const int nat = mv.nat, a = gA - mv.a0;
+  const double *dp = B.dpair + 3 * B.pair_off[id];
   double gx = 0.0, gy = 0.0, gz = 0.0;
-  for (int b = 0; b < mv.nat; ++b) {
-    if (b == a) continue;
-    const int l1 = min(a, b), l2 = max(a, b);
-    const int a1 = mv.a0 + l1, a2 = mv.a0 + l2;
-    const int s1 = B.species[a1], s2 = B.species[a2];
-    const double bx = B.xyz[3 * a2] - B.xyz[3 * a1];
-    const double by = B.xyz[3 * a2 + 1] - B.xyz[3 * a1 + 1];
-    const double bz = B.xyz[3 * a2 + 2] - B.xyz[3 * a1 + 2];
-    const PairDev &P = M.pair[s1 * M.nsp + s2];
-    if (bx * bx + by * by + bz * bz > P.sk_cut * P.sk_cut) continue;
-    for (int kq = 0; kq < 3; ++kq)
-      for (int ii = 0; ii < 2; ++ii) {
-        double v[3] = {bx, by, bz};
-        v[kq] -= (double)(2 * (ii + 1) - 3) * delta;
-        eval_blocks(M, s1, s2, v[0], v[1], v[2], ws_all[w][kq * 2 + ii], lane);
-      }
-    const int o1 = B.a_orb[a1] - mv.o0, o2 = B.a_orb[a2] - mv.o0;
-    const int n1 = M.sp[s1].n_orb, n2 = M.sp[s2].n_orb;
-    const double vs = 0.5 * (Vo[l1] + Vo[l2]);
-    double dt[3] = {0.0, 0.0, 0.0};
-    for (int idx = lane; idx < n1 * n2; idx += 32) {
-      const int bb = idx % n2, aa = idx / n2;
-      const double rv = rho[(o2 + bb) + (size_t)(o1 + aa) * n];
-      const double wv = W[(o2 + bb) + (size_t)(o1 + aa) * n];
-#pragma unroll
-      for (int kq = 0; kq < 3; ++kq) {
-        const double dh = (ws_all[w][2 * kq + 1].blk[0][bb][aa] - ws_all[w][2 * kq].blk[0][bb][aa]) * inv2d;
-        const double ds = (ws_all[w][2 * kq + 1].blk[1][bb][aa] - ws_all[w][2 * kq].blk[1][bb][aa]) * inv2d;
-        dt[kq] += 2.0 * (rv * dh - wv * ds) + 2.0 * vs * ds * rv;
-      }
+  if (lane == 0) {
+    for (int b = 0; b < nat; ++b) {
+      if (b == a) continue;
+      const int l1 = min(a, b), l2 = max(a, b);
+      const long long p = (long long)l1 * (2 * nat - l1 - 1) / 2 + (l2 - l1 - 1);
+      const double sgn = (a == l1) ? 1.0 : -1.0;
+      gx += sgn * dp[3 * p];
+      gy += sgn * dp[3 * p + 1];
+      gz += sgn * dp[3 * p + 2];
     }
-    __syncwarp();
-    const double sgn = (a == l1) ? 1.0 : -1.0;
-    gx += sgn * warp_sum(dt[0]);
-    gy += sgn * warp_sum(dt[1]);
-    gz += sgn * warp_sum(dt[2]);
   }
   // double counting + repulsive
   const int sa = B.species[gA];
@@ -1294,7 +1324,7 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
   if (atom_off[0] != 0) return fail(msg, len, DFTBGPU_ERR_ARGS, "batch: atom_off[0] must be 0");
   const int natom = atom_off[nmol];
   std::vector<int> orb_off(nmol + 1, 0), a_orb(natom), a_mol(natom), o_atom;
-  std::vector<long long> mat_off(nmol + 1, 0), gam_off(nmol + 1, 0);
+  std::vector<long long> mat_off(nmol + 1, 0), gam_off(nmol + 1, 0), pair_off(nmol + 1, 0);
   char buf[256];
   for (int i = 0; i < nmol; ++i) {
     const int na = atom_off[i + 1] - atom_off[i];
@@ -1321,6 +1351,7 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     orb_off[i + 1] = orb_off[i] + no;
     mat_off[i + 1] = mat_off[i] + (long long)no * no;
     gam_off[i + 1] = gam_off[i] + (long long)na * na;
+    pair_off[i + 1] = pair_off[i] + (long long)na * (na - 1) / 2;
   }
   const int norb = orb_off[nmol];
   std::vector<int> order(nmol);
@@ -1329,7 +1360,8 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     return orb_off[x + 1] - orb_off[x] > orb_off[y + 1] - orb_off[y];
   });
   const bool grow = (size_t)nmol > b.cap_mol || (size_t)natom > b.cap_atom || (size_t)norb > b.cap_orb ||
-                    (size_t)mat_off[nmol] > b.cap_mat || (size_t)gam_off[nmol] > b.cap_gam;
+                    (size_t)mat_off[nmol] > b.cap_mat || (size_t)gam_off[nmol] > b.cap_gam ||
+                    (size_t)pair_off[nmol] > b.cap_pair;
   BatchDev &d = b.d;
   if (grow) {
     free_list(b.owned);
@@ -1343,6 +1375,8 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     e |= balloc(b, &ip, NM + 1, b.owned); d.orb_off = ip;
     e |= balloc(b, &lp, NM + 1, b.owned); d.mat_off = lp;
     e |= balloc(b, &lp, NM + 1, b.owned); d.gam_off = lp;
+    e |= balloc(b, &lp, NM + 1, b.owned); d.pair_off = lp;
+    e |= balloc(b, &d.dpair, 3 * (size_t)std::max(pair_off[nmol], 1LL), b.owned);
     e |= balloc(b, &ip, NM, b.owned); d.order = ip;
     e |= balloc(b, &ip, NA, b.owned); d.a_orb = ip;
     e |= balloc(b, &ip, NA, b.owned); d.a_mol = ip;
@@ -1364,7 +1398,7 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     e |= balloc(b, &b.d_active, 1, b.owned);
     if (e) {
       free_list(b.owned);
-      b.cap_mol = b.cap_atom = b.cap_orb = b.cap_mat = b.cap_gam = 0;
+      b.cap_mol = b.cap_atom = b.cap_orb = b.cap_mat = b.cap_gam = b.cap_pair = 0;
       return fail(msg, len, DFTBGPU_ERR_CUDA, "batch: device allocation failed");
     }
     b.cap_mol = NM;
@@ -1372,6 +1406,7 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
     b.cap_orb = NO;
     b.cap_mat = MM;
     b.cap_gam = NG;
+    b.cap_pair = (size_t)pair_off[nmol];
   }
   b.nmol = d.nmol = nmol;
   b.natom = d.natom = natom;
@@ -1391,6 +1426,7 @@ int batch_set_geometries(cudaStream_t s, BatchState &b, const ModelDev &m, const
   acc(up(d.orb_off, orb_off.data(), sizeof(int) * (nmol + 1)));
   acc(up(d.mat_off, mat_off.data(), sizeof(long long) * (nmol + 1)));
   acc(up(d.gam_off, gam_off.data(), sizeof(long long) * (nmol + 1)));
+  acc(up(d.pair_off, pair_off.data(), sizeof(long long) * (nmol + 1)));
   acc(up(d.order, order.data(), sizeof(int) * nmol));
   acc(up(d.a_orb, a_orb.data(), sizeof(int) * natom));
   acc(up(d.a_mol, a_mol.data(), sizeof(int) * natom));
@@ -1480,8 +1516,9 @@ int batch_scc(cudaStream_t s, BatchState &b, const ModelDev &m, const BatchOpts 
 int batch_gradients(cudaStream_t s, BatchState &b, const ModelDev &m, char *msg, size_t len) {
   if (!b.have_scc) return fail(msg, len, DFTBGPU_ERR_STATE, "batch: call the batched SCC first");
   batch_ew_kernel<<<b.nmol, kBatchThreads, 0, s>>>(b.d);
+  batch_pair_grad_kernel<<<b.nmol, 128, 0, s>>>(m, b.d);
   batch_grad_kernel<<<(b.natom + 1) / 2, 64, 0, s>>>(m, b.d);
-  count_launch(2);
+  count_launch(3);
   b.have_w = true;
   const cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return fail(msg, len, DFTBGPU_ERR_CUDA, cudaGetErrorString(ce));

@@ -30,6 +30,7 @@ struct BatchDev {
   const int *atom_off, *orb_off;    // [nmol + 1]
   const long long *mat_off;         // [nmol + 1] offsets of the per-molecule n x n matrices
   const long long *gam_off;         // [nmol + 1] offsets of the per-molecule nat x nat gamma
+  const long long *pair_off;        // [nmol + 1] offsets of the per-molecule atom pairs (i < j)
   const int *a_orb;                 // [natom] global orbital offset of each atom
   const int *a_mol;                 // [natom] molecule of each atom
   const int *o_atom;                // [norb] atom of each orbital (global indices)
@@ -47,6 +48,7 @@ struct BatchDev {
   double *eig, *fill, *dd, *ee;
   // per-atom vectors
   double *q0, *qin, *qout, *V, *Vout, *grad, *erep;
+  double *dpair;                    // band-term gradient of each atom pair (3 per pair, for atom i)
   // Broyden (modified Broyden, one mixer per molecule): ww, aa, beta, cc per molecule (M, M^2, M^2,
   // M); dF, uu per molecule as nat x M blocks at atom_off * M; qlast, dlast per atom
   double *ww, *aa, *beta, *cc, *dF, *uu, *qlast, *dlast;
@@ -62,7 +64,7 @@ struct BatchOpts {
 struct BatchState {
   int nmol = 0, natom = 0, norb = 0, M = 0;
   long long nmat = 0, ngam = 0;
-  size_t cap_atom = 0, cap_orb = 0, cap_mat = 0, cap_gam = 0, cap_mol = 0, cap_M = 0;
+  size_t cap_atom = 0, cap_orb = 0, cap_mat = 0, cap_gam = 0, cap_mol = 0, cap_M = 0, cap_pair = 0;
   std::vector<int> h_atom_off, h_orb_off, h_species;
   std::vector<long long> h_mat_off;
   BatchDev d{};

@@ -30,9 +30,12 @@ static __device__ double neville8(const double *col, double incr, double x, int 
     xp[ii] = (double)(il - 8 + ii + 1) * incr;
     c[ii] = d[ii] = col[il - 8 + ii];
   }
+  // 1 / (xp[mm] - xp[0]) = 1 / (mm incr): one reciprocal and constant factors instead of seven
+  // divisions (a division is a long FP64 sequence on this GPU)
   double delta[8];
+  const double inv_incr = 1.0 / incr;
 #pragma unroll
-  for (int mm = 1; mm < 8; ++mm) delta[mm] = 1.0 / (xp[mm] - xp[0]);
+  for (int mm = 1; mm < 8; ++mm) delta[mm] = inv_incr * (1.0 / (double)mm);
   int icl = (int)ceil((x - xp[0]) * delta[1]);  // 1-based
   icl = max(1, min(8, icl));                     // only binds for r < 4 grid steps (no valid pair)
   double y = col[il - 8 + icl - 1];
