@@ -118,3 +118,36 @@ def test_batch_state_errors(gpu_lib, water_model):
         ctx.batch_scc(binding.default_opts(kT=1e-3, scc_tol=1e-7))
     assert e.value.code == 7
     ctx.close()
+
+
+def test_batch_mixed_spd_fractional(gpu_lib, tio2_model):
+    """Mixed batched form (FP32, FP64 reference, perturbative updates) on Ti/O molecules at high kT."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(8)
+    mols = []
+    while len(mols) < 6:
+        nat = int(rng.integers(3, 8))
+        pts = []
+        while len(pts) < nat:
+            p = rng.uniform(-4.0, 4.0, 3)
+            if all(np.linalg.norm(p - q) > 3.3 for q in pts):
+                pts.append(p)
+        c = np.array(pts).T
+        s = rng.integers(0, 2, nat)
+        _, S = O.build_h0_s(O.System(tio2_model, c, s))
+        if np.linalg.eigvalsh(S)[0] > 0.05:
+            mols.append((c, s))
+    ctx = _ctx(tio2_model)
+    ctx.batch_set_geometries([m[0] for m in mols], [m[1] for m in mols])
+    res = ctx.batch_scc(binding.default_opts(kT=5e-3, scc_tol=1e-7, precision=binding.PREC_MIXED,
+                                             mixed_switch_tol=1e-2))
+    grads = ctx.batch_gradients()
+    for i, (c, s) in enumerate(mols):
+        sys_ = O.System(tio2_model, c, s)
+        ref = O.run_scc(sys_, kt=5e-3, scc_tol=1e-7)
+        if not ref.converged:
+            continue
+        assert res["converged"][i]
+        assert abs(res["energies"][i]["EMermin"] - ref.energies["EMermin"]) / len(s) < 1e-8
+        assert np.max(np.abs(grads[i] - O.gradients(sys_, ref))) < 1e-6
+    ctx.close()

@@ -232,3 +232,30 @@ def test_calculator_api(gpu_lib, water_model):
     q0 = O.System(water_model, c, s).q0_atom
     assert np.max(np.abs(calc.get_gross_charges() - (q0 - ref.q_out_atom))) < Q_TOL
     calc.close()
+
+
+def test_mixed_precision_fractional_spd(gpu_lib, tio2_model):
+    """Mixed form on a Ti/O cluster at high kT: fractional fillings through the perturbative updates
+    (Fermi divided differences, the Fermi-level shift), against the FP64 oracle."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(12)
+    pts = []
+    while len(pts) < 9:
+        p = rng.uniform(-4.5, 4.5, 3)
+        if all(np.linalg.norm(p - q) > 3.3 for q in pts):
+            pts.append(p)
+    c = np.array(pts).T
+    s = np.array([0, 1, 1, 0, 1, 1, 0, 1, 1])
+    sys_ = O.System(tio2_model, c, s)
+    _, S = O.build_h0_s(sys_)
+    if np.linalg.eigvalsh(S)[0] < 0.05:
+        pytest.skip("random geometry gives an ill-conditioned overlap")
+    ref = O.run_scc(sys_, kt=5e-3, scc_tol=1e-7)
+    ctx = _ctx(tio2_model, c, s)
+    res = ctx.scc(binding.default_opts(kT=5e-3, scc_tol=1e-7, precision=binding.PREC_MIXED,
+                                       mixed_switch_tol=1e-2))
+    hist = ctx.scc_history()
+    assert res["converged"] and hist["precision"][-1] == binding.PREC_FP64
+    assert abs(res["energies"]["EMermin"] - ref.energies["EMermin"]) / len(s) < 1e-8
+    assert np.max(np.abs(ctx.gradients() - O.gradients(sys_, ref))) < 1e-6
+    ctx.close()
