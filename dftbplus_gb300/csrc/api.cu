@@ -752,16 +752,26 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->C, n, kALower | kBLower | kCLower);
       add_half_lower(s, n, c->A0, c->C, c->H);
       const bool reference = mixed && !verify;
-      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true, /*all_vectors=*/reference));
+      // FP64 back-transformation of the occupied vectors only; the reference's virtual vectors are
+      // consumed in FP32 by the perturbative updates and are back-transformed in FP32 below
+      DG_CHECK(c, eigensolve(c, n, c->H, pick, /*reduced=*/true, /*all_vectors=*/false));
       k = (int)h_scal[kSNLevels];
       mark(c, kPhDensity);
       prof_flops(c, kPhDensity, (double)n * n * k);
       DG_CHECK(c, density(c, n, k, c->fill, c->rho));
       if (reference) {
-        // reference of the perturbative iterations: C (FP32), X = S C = L Y (FP32), rho, V
+        // reference of the perturbative iterations: C (FP32), X = S C = L Y (FP32), rho, V.
+        // Z holds Y for the first k columns and tridiagonal eigenvectors for the rest.
         mark(c, kPhPert);
-        convert_d2f(s, (size_t)n * n, c->C, c->C32);
+        const size_t nk = (size_t)n * k;
         convert_d2f(s, (size_t)n * n, c->Z, c->Z32);
+        convert_d2f(s, nk, c->C, c->C32);
+        if (k < n) {
+          convert_d2f(s, (size_t)n * n, c->Vh, c->T32);
+          convert_d2f(s, (size_t)n, c->tau, c->tau32);
+          ormtr_left<float>(s, n, n - k, c->T32, n, c->tau32, c->Z32 + nk, n, c->wk32_ormtr);
+          gemm<float>(s, 'T', 'N', n, n - k, n, 1.f, c->Li32, n, c->Z32 + nk, n, 0.f, c->C32 + nk, n, kAUpper);
+        }
         gemm<float>(s, 'N', 'N', n, n, n, 1.f, c->L32, n, c->Z32, n, 0.f, c->V32, n, kALower);
         DG_CUDA(c, cudaMemcpyAsync(c->rho_ref, c->rho, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, s));
         DG_CUDA(c, cudaMemcpyAsync(c->Vref, c->d_V, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
