@@ -180,6 +180,22 @@ def gemm_peak(dtype_name="float64"):
     return 2.0 * n ** 3 / best / 1e12
 
 
+BF16_PEAK_FALLBACK = 1700.0
+BF16_PEAK_SOURCE = "measured sustained cuBLAS bf16 GEMM (MEASURED_PEAKS.json bf16_tflops_sustained)"
+
+
+def bf16_peak():
+    """Dense BF16 tensor peak of this GPU pool (TFLOP/s): the measured sustained figure (the GEMMs run
+    inside a seconds-long step), else the fallback of an earlier GB300 measurement."""
+    global BF16_PEAK_SOURCE
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops_sustained"])
+    except (OSError, KeyError, ValueError):
+        BF16_PEAK_SOURCE = "fallback: 1.7 PFLOP/s sustained bf16 of an earlier GB300 measurement"
+        return BF16_PEAK_FALLBACK
+
+
 def cpu_scc_iteration_time(name, reps=1):
     """Seconds of one SCC iteration of the CPU oracle at full size (H assembly, dsygvd, density
     matrix, Mulliken, potentials), on all host cores."""
@@ -522,11 +538,15 @@ def run_gpu(args):
 
     if rank != 0:
         return
-    # roofline of the dominant GEMM class (FP64 or FP32) against the library GEMM rate measured now
-    g64p, g32p = prof["gemm_fp64"], prof["gemm_fp32"]
-    use32 = g32p["ms"] > g64p["ms"]
-    g = g32p if use32 else g64p
-    peak = gemm_peak("float32" if use32 else "float64")
+    # roofline of the dominant GEMM class: FP64 FMA and FP32 FMA GEMMs against the library GEMM rate
+    # measured now, the tensor-core FP64 digit-slice products (36 BF16 products per FP64 product)
+    # against the measured sustained BF16 tensor peak
+    classes = {"fp64": prof["gemm_fp64"], "fp32": prof["gemm_fp32"], "tc_fp64": prof["gemm_tc_fp64"]}
+    dom = max(classes, key=lambda k: classes[k]["ms"])
+    use32 = dom == "fp32"
+    g = classes[dom]
+    peak = gemm_peak("float32") if use32 else (bf16_peak() if dom == "tc_fp64" else gemm_peak("float64"))
+    peak64 = gemm_peak("float64") if dom != "fp64" else peak
     cpu = None
     if not args.no_cpu_baseline:
         ncpu = os.cpu_count() or 1
@@ -541,8 +561,19 @@ def run_gpu(args):
     if not args.no_batch and world == 1:
         bout, be2e, bseq, bmols = batch_measure(dev)
         bcpu = None if args.no_cpu_baseline else cpu_batch_rate(bmols)
-        batched = _batch_summary(bout, be2e, bseq, bcpu, peak if not use32 else gemm_peak("float64"))
-    achieved = g["flops"] / (g["ms"] / 1e3) / 1e12 if g["ms"] > 0 else 0.0
+        batched = _batch_summary(bout, be2e, bseq, bcpu, peak64)
+    tc_mult = 36.0 if dom == "tc_fp64" else 1.0
+    achieved = tc_mult * g["flops"] / (g["ms"] / 1e3) / 1e12 if g["ms"] > 0 else 0.0
+    gemm_classes = {k: {"ms_per_step": v["ms"] / max(args.steps, 1), "calls_per_step": v["calls"] / max(args.steps, 1),
+                        "fp64_equivalent_tflops": (v["flops"] / (v["ms"] / 1e3) / 1e12) if v["ms"] > 0 else None}
+                    for k, v in classes.items()}
+    kernels = {"fp64": "dgemm_kernel<double> (all FP64 GEMM launches)",
+               "fp32": "dgemm_kernel<float> (FP32 GEMM launches)",
+               "tc_fp64": "dg_gemm_kernel (FP64 products as 36 exact BF16 digit products on tcgen05, "
+                          "with their two packing launches)"}
+    peak_src = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 entry in the measured peaks)",
+                "fp32": "cuBLAS SGEMM (TF32 off) 8192^3 measured in this run (no FP32 entry in the measured peaks)",
+                "tc_fp64": BF16_PEAK_SOURCE}
     phases = {k: round(v["ms"] / max(args.steps, 1), 2) for k, v in prof.items()}
 
     expected_iters = REF_SCC_ITERS.get(args.config)
@@ -555,14 +586,13 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": world * args.steps / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "fp32" if use32 else "fp64",
-                         "kernel": "dgemm_kernel<float> (FP32 GEMM launches)" if use32 else
-                                   "dgemm_kernel<double> (all FP64 GEMM launches)",
+            "roofline": {"bound": "tensor" if dom == "tc_fp64" else dom,
+                         "kernel": kernels[dom],
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
-                         "peak_source": ("cuBLAS SGEMM (TF32 off)" if use32 else "cuBLAS DGEMM") +
-                                        " 8192^3 measured in this run (no FP32/FP64 entry in the measured peaks)",
+                         "peak_source": peak_src[dom],
                          "traffic": None},
+            "gemm_classes": gemm_classes,
             "fp64": fp64,
             "batched": batched,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),

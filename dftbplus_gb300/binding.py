@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(_HERE, "libdftbgpu.so")
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 C_float = C.c_float
+C_double = C.c_double   # for methods whose argument C shadows the ctypes module
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -72,6 +73,9 @@ SIGNATURES = {
     "dftbgpu_test_dgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_double,
                                      _dp, _dp, C.c_double, _dp, C.c_int]),
     "dftbgpu_set_tensor_cores": (C.c_int, [C.c_int]),
+    "dftbgpu_set_fp64_emulation": (C.c_int, [C.c_int]),
+    "dftbgpu_test_dgemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_double,
+                                        _dp, C.c_int, _dp, C.c_int, C.c_double, _dp, C.c_int, C.c_int]),
     "dftbgpu_test_gemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
                                        C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
                                        C.POINTER(C.c_float), C.c_int, C.c_int]),
@@ -83,7 +87,8 @@ SIGNATURES = {
 }
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
-          "density", "mulliken_energy", "broyden", "gradients", "perturbation", "gemm_fp64", "gemm_fp32"]
+          "density", "mulliken_energy", "broyden", "gradients", "perturbation", "gemm_fp64", "gemm_fp32",
+          "gemm_tc_fp64"]
 
 _lib = None
 
@@ -290,6 +295,20 @@ class Context:
                                                  _p(Cm, C_float), m, flags))
         return Cm
 
+    def test_dgemm_tc(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):
+        """C = alpha op(A) op(B) + beta C as exact BF16 digit-slice products on the tensor cores
+        (float64 in and out, column-major)."""
+        A = np.asfortranarray(A, dtype=np.float64)
+        B = np.asfortranarray(B, dtype=np.float64)
+        m = A.shape[1] if ta == "T" else A.shape[0]
+        k = A.shape[0] if ta == "T" else A.shape[1]
+        n = B.shape[0] if tb == "T" else B.shape[1]
+        Cm = np.zeros((m, n), order="F") if C is None else np.array(C, dtype=np.float64, order="F")
+        self.check(self.lib.dftbgpu_test_dgemm_tc(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
+                                                  _p(A, C_double), A.shape[0], _p(B, C_double), B.shape[0], beta,
+                                                  _p(Cm, C_double), m, flags))
+        return Cm
+
     def scc_history(self) -> dict:
         """Per-iteration record of the last SCC call: electronic energy, SCC error, precision form
         (PREC_FP64 / PREC_MIXED for an FP32 eigensolve) and host milliseconds."""
@@ -334,6 +353,12 @@ class Context:
 def set_tensor_cores(enable: bool) -> bool:
     """Route the large FP32 products of the mixed form to the tcgen05 tensor cores (process-wide)."""
     return bool(load_library().dftbgpu_set_tensor_cores(1 if enable else 0))
+
+
+def set_fp64_emulation(enable: bool) -> bool:
+    """Run the mixed form's FP64 products as exact BF16 digit-slice products on the tensor cores
+    (process-wide, on by default); returns the previous setting."""
+    return bool(load_library().dftbgpu_set_fp64_emulation(1 if enable else 0))
 
 
 def default_opts(**kw) -> SccOpts:

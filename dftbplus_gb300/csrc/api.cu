@@ -49,7 +49,8 @@ struct Ctx {
   double *H0 = nullptr, *S = nullptr, *Linv = nullptr, *H = nullptr, *T = nullptr, *Vh = nullptr,
          *Z = nullptr, *C = nullptr, *rho = nullptr, *W = nullptr;
   double *Lc = nullptr;   // Cholesky factor of S (lower)
-  double *A0 = nullptr;   // L^-1 H0 L^-T (lower), per geometry
+  double *A0 = nullptr;   // L^-1 H0 L^-T (lower), per geometry (formed by the first SCC call)
+  bool have_a0 = false;
   // FP32 eigensolver buffers of the mixed form (allocated on first use)
   size_t cap_n32 = 0;
   float *L32 = nullptr, *Li32 = nullptr, *A0_32 = nullptr, *A32 = nullptr, *T32 = nullptr, *V32 = nullptr,
@@ -57,6 +58,7 @@ struct Ctx {
         *wk32_ormtr = nullptr, *wk32_stedc = nullptr;
   bool mixed_ready = false;
   int mixed_iters = 0;    // FP32 iterations of the last SCC call
+  bool scc_mixed = false; // the last SCC call ran the mixed form
   // perturbative iterations of the mixed form: reference density and potentials of the last FP64
   // iteration, M^T / response matrix and C dP (n x n FP32); the FP32 LOW-iteration buffers hold
   // C (C32), X = S C (V32), diag(dV) C (T32), diag(dV) X (Z32) and drho (A32) meanwhile
@@ -127,7 +129,7 @@ static void flush_marks(Ctx *c) {
     cudaEventSynchronize(gp.ev[i + 1]);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, gp.ev[i], gp.ev[i + 1]);
-    const int ph = gp.fp32[i / 2] ? kPhGemm32 : kPhGemm;
+    const int ph = gp.phase[i / 2];
     c->prof_ms[ph] += ms;
     c->prof_flops[ph] += gp.flops[i / 2];
     c->prof_calls[ph] += 1;
@@ -136,7 +138,7 @@ static void flush_marks(Ctx *c) {
   }
   gp.ev.clear();
   gp.flops.clear();
-  gp.fp32.clear();
+  gp.phase.clear();
 }
 
 int set_error(Ctx *c, int code, const char *fmt, ...) {
@@ -291,6 +293,10 @@ static int ensure_mixed(Ctx *c, int n) {
     c->cap_n32 = n;
     c->mixed_ready = false;
   }
+  if (g_tc_dgemm_mixed) {
+    const int e = tc_dgemm_reserve(n, n, n);
+    if (e != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tensor-core FP64 workspace: %s", cudaGetErrorString((cudaError_t)e));
+  }
   if (!c->mixed_ready) {
     size_t nn = (size_t)n * n;
     convert_d2f(c->stream, nn, c->Lc, c->L32);
@@ -361,6 +367,21 @@ static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = fa
     ormtr_left(s, n, kb, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
     dgemm(s, 'T', 'N', n, kb, n, 1.0, c->Linv, n, c->Z, n, 0.0, c->C, n, kAUpper);
   }
+  return DFTBGPU_OK;
+}
+
+// The reduced non-SCC Hamiltonian A0 = L^-1 H0 L^-T (lower), once per geometry, formed by the first
+// SCC call so that the mixed form can run its two products on the tensor cores (g_tc_dgemm set by
+// the caller); the plain form forms it in FP64 arithmetic.
+static int ensure_a0(Ctx *c) {
+  if (c->have_a0) return DFTBGPU_OK;
+  cudaStream_t s = c->stream;
+  const int n = c->norb;
+  mark(c, kPhH0S);
+  prof_flops(c, kPhH0S, 2.0 / 3.0 * (double)n * n * n);
+  dgemm(s, 'N', 'T', n, n, n, 1.0, c->H0, n, c->Linv, n, 0.0, c->T, n, kBUpper);
+  dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->A0, n, kALower | kCLower);
+  c->have_a0 = true;
   return DFTBGPU_OK;
 }
 
@@ -608,8 +629,6 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   potrf_lower(s, norb, c->Lc, norb, c->d_status);
   DG_CHECK(c, check_status(c, "Cholesky of S"));
   trtri_lower(s, norb, c->Lc, norb, c->Linv, norb, c->T, (size_t)norb * norb);
-  dgemm(s, 'N', 'T', norb, norb, norb, 1.0, c->H0, norb, c->Linv, norb, 0.0, c->T, norb, kBUpper);
-  dgemm(s, 'N', 'N', norb, norb, norb, 1.0, c->Linv, norb, c->T, norb, 0.0, c->A0, norb, kALower | kCLower);
   mark(c, -1);
   DG_CUDA(c, cudaGetLastError());
   DG_CUDA(c, cudaStreamSynchronize(s));
@@ -618,6 +637,7 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   c->have_scc = false;
   c->have_w = false;
   c->mixed_ready = false;
+  c->have_a0 = false;
   return DFTBGPU_OK;
 }
 
@@ -668,11 +688,20 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   constexpr int kMaxPertRun = 16;   // perturbative iterations before the reference is renewed
   int pert_run = 0, k_ref = 0;
   bool verify = false;   // the next FULL iteration checks a converged perturbative state (k vectors)
+  g_tc_dgemm = mixed && g_tc_dgemm_mixed;
+  DG_CHECK(c, ensure_a0(c));
+  g_tc_dgemm = false;
   if (mixed) {
     DG_CHECK(c, ensure_mixed(c, n));
     DG_CHECK(c, ensure_pert(c, n, N));
   }
   c->mixed_iters = 0;
+  c->scc_mixed = mixed;
+  // gemm<double> goes to the tensor-core digit-slice product only inside the mixed form's FP64
+  // iterations; the guard switches it off again on every return path
+  struct RouteGuard {
+    ~RouteGuard() { g_tc_dgemm = false; }
+  } route_guard;
   c->hist_e.clear(); c->hist_err.clear(); c->hist_ms.clear(); c->hist_prec.clear();
   int mix_calls = 0;
   auto pick = [&](int *kout) -> int {
@@ -690,6 +719,7 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     const auto t_it = std::chrono::steady_clock::now();
     if (mixed && it == o->max_iter) form = kFormFull;   // the last allowed iteration is FP64
     const int it_form = form;
+    g_tc_dgemm = mixed && g_tc_dgemm_mixed && form == kFormFull;
     mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
     int k = 0;
@@ -790,6 +820,9 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
     DG_CUDA(c, cudaGetLastError());
+    if (mixed && (tc_dgemm_error() || tc_gemm_error()))
+      return set_error(c, DFTBGPU_ERR_ITER_CAP, "tensor-core GEMM: a bounded wait timed out");
+    g_tc_dgemm = false;
     flush_marks(c);
     c->hist_e.push_back(h_scal[kSEnonScc] + h_scal[kSEscc]);
     c->hist_err.push_back(h_scal[kSErr]);
@@ -874,7 +907,10 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
   mark(c, kPhForces);
   prof_flops(c, kPhForces, (double)n * n * c->nlevels);
   energy_weights(s, c->nlevels, c->fill, c->eig, c->fe);
-  DG_CHECK(c, density(c, n, c->nlevels, c->fe, c->W));
+  g_tc_dgemm = c->scc_mixed && g_tc_dgemm_mixed;   // the mixed form's EDM product on the tensor cores
+  const int rc_w = density(c, n, c->nlevels, c->fe, c->W);
+  g_tc_dgemm = false;
+  DG_CHECK(c, rc_w);
   c->have_w = true;
   GeomDev g = geom_view(c);
   ModelDev m = model_view(c);
@@ -925,6 +961,36 @@ int dftbgpu_set_tensor_cores(int enable) {
   const int prev = g_tc_gemm ? 1 : 0;
   g_tc_gemm = enable != 0;
   return prev;
+}
+
+int dftbgpu_set_fp64_emulation(int enable) {
+  const int prev = g_tc_dgemm_mixed ? 1 : 0;
+  g_tc_dgemm_mixed = enable != 0;
+  return prev;
+}
+
+int dftbgpu_test_dgemm_tc(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *a,
+                          int lda, const double *b, int ldb, double beta, double *cm, int ldc, int flags) {
+  if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  const size_t na = (size_t)lda * ((ta == 'N') ? k : m), nb = (size_t)ldb * ((tb == 'N') ? n : k),
+               nc = (size_t)ldc * n;
+  double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  DG_CUDA(c, cudaMalloc((void **)&dA, na * sizeof(double)));
+  DG_CUDA(c, cudaMalloc((void **)&dB, nb * sizeof(double)));
+  DG_CUDA(c, cudaMalloc((void **)&dC, nc * sizeof(double)));
+  DG_CUDA(c, cudaMemcpy(dA, a, na * sizeof(double), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dB, b, nb * sizeof(double), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dC, cm, nc * sizeof(double), cudaMemcpyHostToDevice));
+  const int rc = tc_dgemm(c->stream, ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, flags);
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  DG_CUDA(c, cudaMemcpy(cm, dC, nc * sizeof(double), cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  if (rc != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tc_dgemm: %s", cudaGetErrorString((cudaError_t)rc));
+  if (tc_dgemm_error()) return set_error(c, DFTBGPU_ERR_ITER_CAP, "tc_dgemm: a bounded wait timed out");
+  return DFTBGPU_OK;
 }
 
 int dftbgpu_test_gemm_tc(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, float alpha, const float *a,

@@ -4,6 +4,9 @@
 // These replace the LAPACK/MAGMA calls behind hegvd/magmaHegvd (math/eigensolver.F90:561-660,
 // :1143-1245): potrf + sygst are expressed as a Cholesky factor L, its inverse X = L^-1 and two
 // GEMMs (A = X H X^T), sytrd/ormtr as below, the tridiagonal solve lives in stedc.cu.
+#include <cmath>
+#include <type_traits>
+
 #include "linalg.cuh"
 
 namespace dg {
@@ -174,6 +177,17 @@ static double gemm_executed_flops(int m, int n, int k, int flags) {
   return f;
 }
 
+// The digit-slice product runs one 128 x 64 tile per SM at about 5 us per 64-wide K block; FP64
+// FMA runs about 6e11 multiply-adds/s over the whole GPU. Route a product to the tensor cores only
+// where that estimate says it is faster (few output tiles with a long K stay on FP64).
+static bool tc_dgemm_faster(int m, int n, int k) {
+  const double tiles = (double)ceil_div(m, 128) * ceil_div(n, 64);
+  const double waves = std::ceil(tiles / 148.0);
+  const double t_tc = waves * ceil_div(k, 64) * 5e-6 + 15e-6;
+  const double t_fp64 = (double)m * n * k / 6e11;
+  return t_tc < t_fp64;
+}
+
 template <typename T>
 void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const T *A, int lda, const T *B,
           int ldb, T beta, T *C, int ldc, int flags, T *work, size_t work_elems) {
@@ -202,7 +216,15 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
   }
   T *P = (splits > 1) ? work : nullptr;
   grid.z = splits;
-  const bool done = false;
+  bool done = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (g_tc_dgemm && m >= 64 && n >= 64 && k >= 32 && cap == cudaStreamCaptureStatusNone &&
+        tc_dgemm_faster(m, n, k)) {
+      tc_dgemm(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      done = true;
+      P = nullptr;
+    }
+  }
   if (done) {
   } else if (!TA && !TB)
     dgemm_kernel<T, false, false><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags, P);
@@ -223,7 +245,7 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
     g_gemm_prof.ev.push_back(e0);
     g_gemm_prof.ev.push_back(e1);
     g_gemm_prof.flops.push_back(gemm_executed_flops(m, n, k, flags));
-    g_gemm_prof.fp32.push_back(sizeof(T) == 4);
+    g_gemm_prof.phase.push_back(done ? kPhGemmTc : (sizeof(T) == 4 ? kPhGemm32 : kPhGemm));
   }
 }
 

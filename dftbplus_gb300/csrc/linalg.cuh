@@ -33,6 +33,19 @@ int tc_gemm_error();
 // is scaled down by it; full FP32 eigensolves keep FP32 FMA products.
 extern bool g_tc_gemm;
 
+// FP64-class product on the tensor cores (tc_dgemm.cu): exact BF16 digit-slice products (eight
+// 7-bit digits per element, integer accumulation), same arguments and flags as gemm. Returns a
+// cudaError_t value. tc_dgemm_reserve sizes its workspace ahead of use.
+int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+             const double *B, int ldb, double beta, double *C, int ldc, int flags);
+int tc_dgemm_reserve(int m, int n, int k);
+int tc_dgemm_error();
+// While g_tc_dgemm is set, gemm<double> sends products with m, n >= 64 and k >= 32 to tc_dgemm
+// where a cost estimate favours it (the mixed form sets it around its FP64 iterations when
+// g_tc_dgemm_mixed allows it).
+extern bool g_tc_dgemm;
+extern bool g_tc_dgemm_mixed;
+
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
            double *work = nullptr, size_t work_elems = 0);
@@ -44,7 +57,8 @@ struct GemmProfile {
   bool on = false;
   std::vector<cudaEvent_t> ev;     // pairs (start, stop)
   std::vector<double> flops;       // per pair
-  std::vector<bool> fp32;          // per pair: FP32 instead of FP64
+  std::vector<int> phase;          // per pair: kPhGemm (FP64), kPhGemm32 (FP32) or kPhGemmTc
+                                   // (FP64 as tensor-core digit-slice products)
 };
 extern GemmProfile g_gemm_prof;
 

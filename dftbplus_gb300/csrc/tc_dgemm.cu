@@ -1,0 +1,393 @@
+// FP64-class GEMM on the tcgen05 tensor cores (sm_103a): C = alpha op(A) op(B) + beta C for FP64
+// operands, computed exactly on BF16 digit slices (an Ozaki-type splitting). GB300 issues FP64 FMAs
+// at about 2 per clock per SM, its BF16 tensor cores about 4,000 multiply-adds per clock per SM, so
+// 36 exact BF16 digit products still run well ahead of FP64 arithmetic.
+//
+// Splitting. Row i of op(A) gets a power-of-two scale 2^EA_i > max_k |A_ik|. Each element is
+// rounded to the 55-bit fixed-point integer Y = round(|A_ik| 2^(55 - EA_i)) and recoded into eight
+// signed 7-bit digits, A_ik = sign 2^(EA_i - 55) sum_s a_s 2^(7 (7 - s)) with a_0 in [0, 64] and
+// a_s in [-64, 63] for s >= 1, so every digit is an integer that BF16 holds exactly. Columns of
+// op(B) are split the same way (EB_j). Rounding Y is the only approximation of the operands: at most
+// 2^-56 of the row (column) maximum.
+//
+// Products. The digit products with s + t = g are summed into one tensor-memory accumulator per
+// group g = 0..7 (36 products; the groups g >= 8 lie 2^-56 below the leading one and are dropped).
+// Over one K-block of 64 each group sum is an integer of magnitude <= 8 * 64 * 2^12 = 2^21, so the
+// FP32 accumulation in tensor memory is exact whatever its rounding. After each K-block the eight
+// sums are read back, converted to int32 exactly (magic-number addition) and added into one int64
+// fixed-point accumulator per output element with weights 2^(7 (7 - g) - R); R = ceil(log2 Kp) - 1
+// keeps the int64 clear of overflow (the weights of groups 6 and 7 become rounding right shifts: at
+// most half a unit of 2^(EA_i + EB_j - 61 + R) per K-block and group). The epilogue scales the int64
+// by 2^(EA_i + EB_j - 61 + R) in FP64. Integer accumulation makes the result independent of the
+// order of the K-blocks.
+//
+// Accuracy: the error of C_ij is below K max_k|A_ik| max_k|B_kj| (2^-53 + K 2^-65), FP64-class
+// (a native FP64 GEMM's bound is K 2^-53 sum_k |A_ik| |B_kj|); a row or column of op(A), op(B) that
+// holds Inf or NaN gives NaN outputs.
+//
+// Kernel: one 128 x 64 output tile per CTA (256 threads). Per K-block the 8 + 8 digit slabs of the
+// A and B tiles (192 KB) are copied with cp.async into 128-byte-swizzled shared memory, one thread
+// issues the 144 tcgen05.mma (36 products x 4 K-steps of 16, M = 128, N = 64) into eight 64-column
+// TMEM accumulators and commits them to an mbarrier; after the bounded wait the next K-block's copies
+// are started and the eight warps read the group sums back (two warps per 32-lane TMEM quadrant, 32
+// columns each). Every wait is bounded; on a timeout the kernel records an error, skips the output
+// and releases its TMEM.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <type_traits>
+
+#include "linalg.cuh"
+#include "tcgen05.cuh"
+
+namespace dg {
+
+constexpr int DG_S = 8;                                   // digits per element
+constexpr int DG_BM = 128, DG_BN = 64, DG_BK = 64;
+constexpr int DG_THREADS = 256;
+constexpr int DG_ATILE = DG_BM * DG_BK * 2;               // 16 KB: one digit slab of the A tile
+constexpr int DG_BTILE = DG_BN * DG_BK * 2;               // 8 KB: one digit slab of the B tile
+constexpr int DG_STAGE = DG_S * (DG_ATILE + DG_BTILE);    // 192 KB
+constexpr int DG_SMEM = DG_STAGE + 1024 + 64;             // alignment slack + barrier, TMEM slot, flag
+constexpr uint32_t DG_TMEM_COLS = 512;                    // 8 groups x 64 columns
+
+// Scale exponent E of a row from the bit pattern of its largest magnitude: max < 2^E.
+__device__ __forceinline__ int dg_row_exp(unsigned long long maxbits) {
+  const int ex = (int)(maxbits >> 52);
+  return (ex < 1 ? 1 : ex) - 1022;
+}
+
+// Eight signed 7-bit digits of x at scale 2^E (see the header): x ~ 2^(E-55) sum_s d_s 2^(7(7-s)).
+__device__ __forceinline__ void dg_digits(double x, int E, int *d) {
+  const long long bits = __double_as_longlong(x);
+  const unsigned long long ab = (unsigned long long)bits & 0x7FFFFFFFFFFFFFFFull;
+  int ex = (int)(ab >> 52);
+  unsigned long long mant = ab & 0xFFFFFFFFFFFFFull;
+  if (ex) mant |= 1ull << 52;
+  else ex = 1;
+  // |x| = mant 2^(ex - 1075); Y = round(|x| 2^(55 - E)) = round(mant 2^(ex - 1020 - E)) < 2^55
+  const int sh = ex - 1020 - E;
+  unsigned long long Y = 0;
+  if (mant != 0 && ex < 2047) {
+    if (sh >= 0) Y = mant << (sh > 2 ? 2 : sh);   // sh <= 2 whenever |x| < 2^E
+    else if (sh > -64) Y = (mant + (1ull << (-sh - 1))) >> (-sh);
+  }
+#pragma unroll
+  for (int s = DG_S - 1; s >= 1; --s) {
+    int v = (int)(Y & 127ull);
+    v -= (v >= 64) ? 128 : 0;
+    d[s] = v;
+    Y = (Y - (unsigned long long)(long long)v) >> 7;
+  }
+  d[0] = (int)Y;
+  if (bits < 0) {
+#pragma unroll
+    for (int s = 0; s < DG_S; ++s) d[s] = -d[s];
+  }
+}
+
+// ------------------------------------------------------------------------------ packing
+// One block per 32 rows of the operand (rows R, K columns; element (r, k) = src[r * rs + k * ks],
+// zero where the mask marks a structural zero: 1 keeps k <= r, 2 keeps k >= r). Pass 1 finds each
+// row's largest magnitude (written to rmax[r] as its bit pattern), pass 2 writes the eight digit
+// slabs P[s * slab + r * Kp + k] (BF16, K-major, zero-padded to Kp columns and to the block's rows).
+// 32 x 32 tiles through shared memory keep both the reads and the writes coalesced.
+__global__ void __launch_bounds__(256) dg_pack_kernel(int R, int K, const double *src, long long rs, long long ks,
+                                                      int mask, int Kp, size_t slab, __nv_bfloat16 *P,
+                                                      unsigned long long *rmax) {
+  __shared__ double tile[32][33];
+  __shared__ unsigned long long smax[32];
+  const int r0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool k_contig = (ks == 1);
+  auto load_tile = [&](int k0) {
+#pragma unroll
+    for (int q = ty; q < 32; q += 8) {
+      const int r = k_contig ? r0 + q : r0 + tx;
+      const int k = k_contig ? k0 + tx : k0 + q;
+      double v = 0.0;
+      if (r < R && k < K) {
+        const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
+        if (keep) v = src[(long long)r * rs + (long long)k * ks];
+      }
+      if (k_contig) tile[q][tx] = v;
+      else tile[tx][q] = v;
+    }
+  };
+  unsigned long long mx[4] = {0ull, 0ull, 0ull, 0ull};
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    __syncthreads();
+    load_tile(k0);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const unsigned long long b =
+          (unsigned long long)__double_as_longlong(tile[ty + 8 * i][tx]) & 0x7FFFFFFFFFFFFFFFull;
+      mx[i] = b > mx[i] ? b : mx[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    unsigned long long v = mx[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w > v ? w : v;
+    }
+    if (tx == 0) smax[ty + 8 * i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) rmax[r0 + threadIdx.x] = smax[threadIdx.x];
+  int E[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) E[i] = dg_row_exp(smax[ty + 8 * i]);
+  for (int k0 = 0; k0 < Kp; k0 += 32) {
+    __syncthreads();
+    load_tile(k0);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int q = ty + 8 * i;
+      int d[DG_S];
+      dg_digits(tile[q][tx], E[i], d);
+      __nv_bfloat16 *dst = P + (size_t)(r0 + q) * Kp + k0 + tx;
+#pragma unroll
+      for (int s = 0; s < DG_S; ++s) dst[(size_t)s * slab] = __float2bfloat16_rn((float)d[s]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ kernel
+// Instruction descriptor: D FP32, A and B BF16, both K-major, M = 128, N = 64.
+__host__ __device__ constexpr uint32_t dg_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(DG_BN >> 3) << 17) | ((uint32_t)(DG_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+// Exact int32 of an FP32 integer v with |v| < 2^22: v + 1.5 * 2^23 keeps v in the low mantissa bits.
+__device__ __forceinline__ int dg_exact_int(uint32_t vbits) {
+  return __float_as_int(__uint_as_float(vbits) + 12582912.0f) - 0x4B400000;
+}
+
+// Packed operands: PA = eight digit slabs of op(A) rows (each Mp x Kp), PB = eight slabs of op(B)^T
+// rows (each Np x Kp); rmaxA / rmaxB the row maxima of the packing pass.
+__global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, int Kp, int Mp, int Np,
+                                                              const __nv_bfloat16 *PA, const __nv_bfloat16 *PB,
+                                                              const unsigned long long *rmaxA,
+                                                              const unsigned long long *rmaxB, int R, double alpha,
+                                                              double beta, double *C, int ldc, int flags, int *err) {
+  extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int i0 = blockIdx.x * DG_BM, j0 = blockIdx.y * DG_BN;
+  if ((flags & kCLower) && j0 > i0 + DG_BM - 1) return;   // tile above the diagonal, before any TMEM use
+  // K-blocks that can hold non-zero products (triangular operands), as in the FP64 GEMM
+  int kbeg = 0, kend = Kp;
+  if (flags & kALower) kend = min(kend, i0 + DG_BM);
+  if (flags & kAUpper) kbeg = max(kbeg, i0);
+  if (flags & kBLower) kbeg = max(kbeg, j0);
+  if (flags & kBUpper) kend = min(kend, j0 + DG_BN);
+  const int kb0 = kbeg / DG_BK, kb1 = (kend + DG_BK - 1) / DG_BK;
+  const int nkb = kb1 > kb0 ? kb1 - kb0 : 0;
+
+  const uint32_t raw = smem_u32(dg_smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  unsigned char *sm = dg_smem_raw + (base - raw);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + DG_STAGE);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + DG_STAGE + 8);
+  volatile int *sfail = reinterpret_cast<volatile int *>(sm + DG_STAGE + 16);
+  if (t == 0) {
+    mbar_init(smem_u32(mbar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sfail = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(DG_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const size_t slabA = (size_t)Mp * Kp, slabB = (size_t)Np * Kp;
+  // 8 A slabs x 128 rows x 8 chunks of 16 B, then 8 B slabs x 64 rows x 8 chunks: 48 per thread
+  auto prefetch = [&](int kb) {
+#pragma unroll
+    for (int q = 0; q < 48; ++q) {
+      const int c = t + q * DG_THREADS;
+      const __nv_bfloat16 *g;
+      uint32_t dst;
+      if (q < 32) {
+        const int sl = c >> 10, r = (c >> 3) & 127, ch = c & 7;
+        g = PA + (size_t)sl * slabA + (size_t)(i0 + r) * Kp + (size_t)kb * DG_BK + ch * 8;
+        dst = base + sl * DG_ATILE + r * 128 + ((ch ^ (r & 7)) << 4);
+      } else {
+        const int cb = c - 8192;
+        const int sl = cb >> 9, r = (cb >> 3) & 63, ch = cb & 7;
+        g = PB + (size_t)sl * slabB + (size_t)(j0 + r) * Kp + (size_t)kb * DG_BK + ch * 8;
+        dst = base + DG_S * DG_ATILE + sl * DG_BTILE + r * 128 + ((ch ^ (r & 7)) << 4);
+      }
+      cp_async16(dst, g);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+
+  const int quad = warp & 3, half = warp >> 2;
+  long long acc[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) acc[c] = 0;
+  if (nkb > 0) prefetch(kb0);
+  for (int it = 0; it < nkb; ++it) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int g = 0; g < DG_S; ++g)
+#pragma unroll
+        for (int s = 0; s <= g; ++s)
+#pragma unroll
+          for (int kk = 0; kk < DG_BK / 16; ++kk)
+            tc_mma(tmem + (uint32_t)(g * DG_BN), tc_sdesc(base + s * DG_ATILE + kk * 32),
+                   tc_sdesc(base + DG_S * DG_ATILE + (g - s) * DG_BTILE + kk * 32), dg_idesc(),
+                   (s | kk) != 0 ? 1u : 0u);
+      tc_commit(smem_u32(mbar));
+      if (!mbar_wait(smem_u32(mbar), (uint32_t)(it & 1))) *sfail = 1;
+    }
+    __syncthreads();
+    if (*sfail) break;
+    if (it + 1 < nkb) prefetch(kb0 + it + 1);   // shared memory is free once the MMAs completed
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+    for (int g = 0; g < DG_S; ++g) {
+      uint32_t v[32];
+      tc_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(g * DG_BN + half * 32), v);
+      const int sh = 7 * (DG_S - 1 - g) - R;
+      if (sh >= 0) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] += (long long)dg_exact_int(v[c]) << sh;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] += (long long)((dg_exact_int(v[c]) + (1 << (-sh - 1))) >> (-sh));
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+  const bool failed = *sfail != 0;
+  if (failed && t == 0) mbar_wait(smem_u32(mbar), (uint32_t)((nkb - 1) & 1));   // let in-flight MMAs drain
+  if (!failed) {
+    const int row = i0 + quad * 32 + lane;
+    if (row < m) {
+      const unsigned long long ma = rmaxA[row];
+      const int ea = dg_row_exp(ma) - 61 + R;
+      const bool bad_a = (ma >> 52) >= 2047ull;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int col = j0 + half * 32 + c;
+        if (col < n && (!(flags & kCLower) || row >= col)) {
+          const unsigned long long mb = rmaxB[col];
+          double x = ldexp((double)acc[c], ea + dg_row_exp(mb));
+          if (bad_a || (mb >> 52) >= 2047ull) x = __longlong_as_double(0x7FF8000000000000ll);
+          x *= alpha;
+          double *cp = C + row + (size_t)col * ldc;
+          if (beta != 0.0) x = fma(beta, *cp, x);
+          *cp = x;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DG_TMEM_COLS) : "memory");
+  }
+  if (t == 0 && failed) atomicExch(err, 1);
+}
+
+// ------------------------------------------------------------------------------ host side
+bool g_tc_dgemm = false;          // gemm<double> routes here while set (the mixed form's FP64 iterations)
+bool g_tc_dgemm_mixed = true;     // dftbgpu_set_fp64_emulation
+static __nv_bfloat16 *g_dg_ws = nullptr;
+static size_t g_dg_ws_elems = 0;
+static unsigned long long *g_dg_rmax = nullptr;
+static size_t g_dg_rmax_elems = 0;
+static int *g_dg_err = nullptr;
+
+static int dg_round_up(int x, int q) { return (x + q - 1) / q * q; }
+
+static int dg_ensure(size_t ws_elems, size_t rmax_elems) {
+  if (ws_elems > g_dg_ws_elems) {
+    cudaDeviceSynchronize();
+    if (g_dg_ws) cudaFree(g_dg_ws);
+    g_dg_ws = nullptr;
+    g_dg_ws_elems = 0;
+    cudaError_t e = cudaMalloc((void **)&g_dg_ws, ws_elems * sizeof(__nv_bfloat16));
+    if (e != cudaSuccess) return (int)e;
+    g_dg_ws_elems = ws_elems;
+  }
+  if (rmax_elems > g_dg_rmax_elems) {
+    cudaDeviceSynchronize();
+    if (g_dg_rmax) cudaFree(g_dg_rmax);
+    g_dg_rmax = nullptr;
+    g_dg_rmax_elems = 0;
+    cudaError_t e = cudaMalloc((void **)&g_dg_rmax, rmax_elems * sizeof(unsigned long long));
+    if (e != cudaSuccess) return (int)e;
+    g_dg_rmax_elems = rmax_elems;
+  }
+  if (!g_dg_err) {
+    cudaError_t e = cudaMalloc((void **)&g_dg_err, sizeof(int));
+    if (e != cudaSuccess) return (int)e;
+    cudaMemset(g_dg_err, 0, sizeof(int));
+    cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM);
+  }
+  return 0;
+}
+
+int tc_dgemm_reserve(int m, int n, int k) {
+  const size_t Mp = (size_t)dg_round_up(m, DG_BM), Np = (size_t)dg_round_up(n, DG_BN),
+               Kp = (size_t)dg_round_up(std::max(k, 1), DG_BK);
+  return dg_ensure((size_t)DG_S * (Mp + Np) * Kp, Mp + Np);
+}
+
+int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+             const double *B, int ldb, double beta, double *C, int ldc, int flags) {
+  if (m <= 0 || n <= 0) return 0;
+  const int Mp = dg_round_up(m, DG_BM), Np = dg_round_up(n, DG_BN), Kp = dg_round_up(std::max(k, 1), DG_BK);
+  int rc = dg_ensure((size_t)DG_S * ((size_t)Mp + (size_t)Np) * Kp, (size_t)Mp + Np);
+  if (rc != 0) return rc;
+  __nv_bfloat16 *PA = g_dg_ws, *PB = PA + (size_t)DG_S * Mp * Kp;
+  unsigned long long *rA = g_dg_rmax, *rB = g_dg_rmax + Mp;
+  const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
+  // op(A)(r, k) and op(B)^T(j, k) as strided views; structural zeros from the triangular flags
+  const long long ars = TA ? lda : 1, aks = TA ? 1 : lda;
+  const long long brs = TB ? 1 : ldb, bks = TB ? ldb : 1;
+  const int amask = (flags & kALower) ? 1 : ((flags & kAUpper) ? 2 : 0);
+  const int bmask = (flags & kBLower) ? 2 : ((flags & kBUpper) ? 1 : 0);
+  dg_pack_kernel<<<Mp / 32, 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, (size_t)Mp * Kp, PA, rA);
+  dg_pack_kernel<<<Np / 32, 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
+  int R = 0;
+  while ((1 << (R + 1)) < Kp) ++R;   // R = ceil(log2 Kp) - 1
+  dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN), DG_THREADS, DG_SMEM, s>>>(m, n, Kp, Mp, Np, PA, PB, rA, rB, R,
+                                                                           alpha, beta, C, ldc, flags, g_dg_err);
+  count_launch(3);
+  return (int)cudaGetLastError();
+}
+
+int tc_dgemm_error() {
+  if (!g_dg_err) return 0;
+  int h = 0;
+  cudaMemcpy(&h, g_dg_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (h) cudaMemset(g_dg_err, 0, sizeof(int));
+  return h;
+}
+
+}  // namespace dg

@@ -206,9 +206,11 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  *   4 tridiagonal divide and conquer, 5 Fermi filling, 6 back-transformation (Q Z, L^-T Y),
  *   7 density matrix, 8 Mulliken + energies, 9 Broyden mixing, 10 gradients, 11 density-matrix
  *   perturbation (mixed form: reference set-up and perturbative updates), 12 FP64 GEMM (all FP64
- *   GEMM launches, overlapping the phases above), 13 FP32 GEMM (mixed form, likewise).
- * enable: 1 resets and starts accumulating, 0 stops. read: ms[14], flops[14] (algorithmic FLOPs
- * per phase as counted for the roofline), calls[14]; returns the number of phases written.
+ *   GEMM launches, overlapping the phases above), 13 FP32 GEMM (mixed form, likewise), 14 FP64
+ *   GEMM as tensor-core digit-slice products (mixed form, likewise; FLOPs counted as the FP64
+ *   product's 2mnk, the tensor cores execute 36 BF16 products of it).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[15], flops[15] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[15]; returns the number of phases written.
  */
 int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);
@@ -247,6 +249,20 @@ int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *st
 int dftbgpu_set_tensor_cores(int enable);
 int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha, const float *a,
                          int lda, const float *b, int ldb, float beta, float *c, int ldc, int flags);
+/*
+ * FP64-class products of the mixed form on the tensor cores (no reference counterpart): when
+ * enabled (the default), the FP64 GEMMs of the mixed form's FP64 iterations (reduced transform,
+ * tridiagonalisation updates, divide-and-conquer merges, back-transformation, density and
+ * energy-weighted density matrices) run as exact products of BF16 digit slices on the tcgen05
+ * tensor cores: eight signed 7-bit digits per element at a power-of-two scale per row (column),
+ * group sums exact in FP32 per 64-wide K block, int64 accumulation. The error is below 2^-52 of
+ * max|A_ik| max|B_kj| K per element, like an FP64 product. The plain FP64 form always uses FP64
+ * arithmetic. Process-wide; returns the previous setting. dftbgpu_test_dgemm_tc runs one such
+ * product on host arrays (column-major, flags as the library's triangular GEMM hints).
+ */
+int dftbgpu_set_fp64_emulation(int enable);
+int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
+                          int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
 int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
                        const double *a, const double *b, double beta, double *c, int flags);
 int dftbgpu_test_tridiag(dftbgpu_ctx *ctx, int n, const double *a, double *d, double *e);

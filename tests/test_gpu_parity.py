@@ -182,6 +182,33 @@ def test_mixed_precision_matches_fp64(gpu_lib, water_model, n_mol, radius, seed)
     ctx.close()
 
 
+def test_mixed_fp64_products_on_tensor_cores(gpu_lib, water_model):
+    """The mixed form's FP64 iterations with their GEMMs as exact digit-slice products on the tensor
+    cores (default) and with FP64 arithmetic: both meet the oracle, and agree with each other."""
+    from dftbplus_gb300 import binding, synth
+    c, s = synth.water_cluster(128, 20.0, 128)
+    sys_ = O.System(water_model, c, s)
+    ref = O.run_scc(sys_, kt=1e-3, scc_tol=1e-7)
+    gref = O.gradients(sys_, ref)
+    out = {}
+    prev = binding.set_fp64_emulation(True)
+    try:
+        for emulate in (True, False):
+            binding.set_fp64_emulation(emulate)
+            ctx = _ctx(water_model, c, s)
+            res = ctx.scc(binding.default_opts(kT=1e-3, scc_tol=1e-7, precision=binding.PREC_MIXED))
+            assert res["converged"]
+            out[emulate] = (res["energies"]["EMermin"], res["q_out"], ctx.gradients())
+            ctx.close()
+    finally:
+        binding.set_fp64_emulation(prev)
+    for e, q, g in out.values():
+        assert abs(e - ref.energies["EMermin"]) / len(s) < 1e-8
+        assert np.max(np.abs(q - ref.q_out_atom)) < 1e-6
+        assert np.max(np.abs(g - gref)) < 1e-6
+    assert abs(out[True][0] - out[False][0]) / len(s) < 1e-9
+
+
 def test_not_positive_definite_reports_status(gpu_lib):
     """A table draw with an indefinite overlap: the Cholesky reports the status, no fault."""
     from dftbplus_gb300 import binding, synth

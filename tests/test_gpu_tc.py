@@ -52,3 +52,74 @@ def test_tc_gemm_flags_and_beta(gpu_lib):
     assert np.all(np.abs(C - ref)[low] <= 2e-6 * mag[low] + 1e-6)
     assert np.array_equal(C[~low], C0[~low])       # upper triangle untouched
     ctx.close()
+
+
+# ------------------------------------------------------------------ FP64-class digit-slice products
+def _dref(ta, tb, A, B):
+    a = A.T if ta == "T" else A
+    b = B.T if tb == "T" else B
+    k = a.shape[1]
+    # error bound of the digit-slice product (K max|a_i.| max|b_.j| (2^-53 + K 2^-65)) plus that of
+    # the float64 reference itself (K 2^-53 sum |a||b| <= K^2 2^-53 max max, kept to the same form)
+    scale = k * np.abs(a).max(1)[:, None] * np.abs(b).max(0)[None, :]
+    return a @ b, scale * (2.0 ** -51 + k * 2.0 ** -64)
+
+
+@pytest.mark.parametrize("m,n,k,ta,tb", [
+    (128, 64, 64, "N", "N"),       # one tile, one K block
+    (256, 192, 200, "N", "N"),     # several tiles and K blocks, ragged K
+    (300, 200, 100, "N", "T"),     # ragged edges, padding
+    (384, 257, 640, "T", "N"),
+    (129, 511, 77, "T", "T"),
+    (96, 40, 32, "N", "N"),        # smaller than one tile
+])
+def test_tc_dgemm_products(gpu_lib, m, n, k, ta, tb):
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(m * 5 + n + k)
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k))
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+    ctx = binding.Context(0)
+    C = ctx.test_dgemm_tc(ta, tb, A, B)
+    ref, tol = _dref(ta, tb, A, B)
+    assert np.all(np.abs(C - ref) <= tol), np.max(np.abs(C - ref) / tol)
+    ctx.close()
+
+
+def test_tc_dgemm_scales_zeros_and_flags(gpu_lib):
+    """Rows and columns over 60 orders of magnitude, zero rows, triangular hints, lower-only output
+    and beta accumulation; the untouched upper triangle keeps its bits."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(11)
+    n = 320
+    L = np.tril(rng.standard_normal((n, n))) * 10.0 ** rng.uniform(-30, 30, (n, 1))
+    L[17] = 0.0
+    junk = np.triu(rng.standard_normal((n, n)), 1)          # must be ignored (kALower)
+    X = rng.standard_normal((n, n)) * 10.0 ** rng.uniform(-5, 5, (1, n))
+    C0 = rng.standard_normal((n, n))
+    ctx = binding.Context(0)
+    kALower, kCLower = 1, 16
+    C = ctx.test_dgemm_tc("N", "N", L + junk, X, C=C0, alpha=0.5, beta=1.0, flags=kALower | kCLower)
+    ref, tol = _dref("N", "N", L, X)
+    ref = 0.5 * ref + C0
+    tol = 0.5 * tol + 2.0 ** -52 * np.abs(C0)
+    low = np.tril(np.ones((n, n), dtype=bool))
+    assert np.all(np.abs(C - ref)[low] <= tol[low]), np.max((np.abs(C - ref) / tol)[low])
+    assert np.array_equal(C[~low], C0[~low])
+    assert np.array_equal(C[17, :18], C0[17, :18])          # zero row: alpha * 0 + beta * C0
+    ctx.close()
+
+
+def test_tc_dgemm_largest_digit_sums(gpu_lib):
+    """Every digit 63 but the last: block group sums near the 2^21 bound must stay exact in the
+    tensor-memory FP32 accumulators (K = 1,024, so 16 K blocks are read back)."""
+    from dftbplus_gb300 import binding
+    Y = 63 * sum(128 ** j for j in range(1, 8))
+    x = Y * 2.0 ** -54
+    k = 1024
+    A = np.full((128, k), x)
+    B = np.full((k, 64), -x)
+    ctx = binding.Context(0)
+    C = ctx.test_dgemm_tc("N", "N", A, B)
+    exact = -k * x * x
+    assert np.all(np.abs(C - exact) <= abs(exact) * 2.0 ** -50)
+    ctx.close()
