@@ -177,15 +177,11 @@ static double gemm_executed_flops(int m, int n, int k, int flags) {
   return f;
 }
 
-// The digit-slice product runs one 128 x 64 tile per SM at about 5 us per 64-wide K block; FP64
-// FMA runs about 6e11 multiply-adds/s over the whole GPU. Route a product to the tensor cores only
-// where that estimate says it is faster (few output tiles with a long K stay on FP64).
+// The digit-slice product runs one 128 x 64 tile per SM at about 5 us per 64-wide K block (split
+// along K when it has few tiles); FP64 FMA runs about 6e11 multiply-adds/s over the whole GPU. Route a
+// product to the tensor cores only where that estimate says it is faster.
 static bool tc_dgemm_faster(int m, int n, int k) {
-  const double tiles = (double)ceil_div(m, 128) * ceil_div(n, 64);
-  const double waves = std::ceil(tiles / 148.0);
-  const double t_tc = waves * ceil_div(k, 64) * 5e-6 + 15e-6;
-  const double t_fp64 = (double)m * n * k / 6e11;
-  return t_tc < t_fp64;
+  return tc_dgemm_estimate_s(m, n, k) < (double)m * n * k / 6e11;
 }
 
 template <typename T>

@@ -39,6 +39,7 @@ extern bool g_tc_gemm;
 int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
              const double *B, int ldb, double beta, double *C, int ldc, int flags);
 int tc_dgemm_reserve(int m, int n, int k);
+double tc_dgemm_estimate_s(int m, int n, int k);   // seconds, for routing
 int tc_dgemm_error();
 // While g_tc_dgemm is set, gemm<double> sends products with m, n >= 64 and k >= 32 to tc_dgemm
 // where a cost estimate favours it (the mixed form sets it around its FP64 iterations when

@@ -14,7 +14,8 @@
 // group g = 0..7 (36 products; the groups g >= 8 lie 2^-56 below the leading one and are dropped).
 // Over one K-block of 64 each group sum is an integer of magnitude <= 8 * 64 * 2^12 = 2^21, so the
 // FP32 accumulation in tensor memory is exact whatever its rounding. After each K-block the eight
-// sums are read back, converted to int32 exactly (magic-number addition) and added into one int64
+// sums are read back, converted to int32 exactly (adding 1.5 * 2^23 leaves an integer |v| <= 2^22 in
+// the low mantissa bits), combined in pairs 2^7 G_g + G_{g+1} (int32) and added into one int64
 // fixed-point accumulator per output element with weights 2^(7 (7 - g) - R); R = ceil(log2 Kp) - 1
 // keeps the int64 clear of overflow (the weights of groups 6 and 7 become rounding right shifts: at
 // most half a unit of 2^(EA_i + EB_j - 61 + R) per K-block and group). The epilogue scales the int64
@@ -167,18 +168,16 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 
-// Exact int32 of an FP32 integer v with |v| < 2^22: v + 1.5 * 2^23 keeps v in the low mantissa bits.
-__device__ __forceinline__ int dg_exact_int(uint32_t vbits) {
-  return __float_as_int(__uint_as_float(vbits) + 12582912.0f) - 0x4B400000;
-}
-
 // Packed operands: PA = eight digit slabs of op(A) rows (each Mp x Kp), PB = eight slabs of op(B)^T
-// rows (each Np x Kp); rmaxA / rmaxB the row maxima of the packing pass.
+// rows (each Np x Kp); rmaxA / rmaxB the row maxima of the packing pass. With P != nullptr the CTA
+// (x, y, z) sums only the z-th run of kb_split K-blocks and stores its raw int64 accumulators at
+// P[z Mp Np + row + col Mp] (split-K; dg_splitk_reduce adds them exactly and scales).
 __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, int Kp, int Mp, int Np,
                                                               const __nv_bfloat16 *PA, const __nv_bfloat16 *PB,
                                                               const unsigned long long *rmaxA,
                                                               const unsigned long long *rmaxB, int R, double alpha,
-                                                              double beta, double *C, int ldc, int flags, int *err) {
+                                                              double beta, double *C, int ldc, int flags, int *err,
+                                                              long long *P, int kb_split) {
   extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int i0 = blockIdx.x * DG_BM, j0 = blockIdx.y * DG_BN;
@@ -189,7 +188,11 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
   if (flags & kAUpper) kbeg = max(kbeg, i0);
   if (flags & kBLower) kbeg = max(kbeg, j0);
   if (flags & kBUpper) kend = min(kend, j0 + DG_BN);
-  const int kb0 = kbeg / DG_BK, kb1 = (kend + DG_BK - 1) / DG_BK;
+  int kb0 = kbeg / DG_BK, kb1 = (kend + DG_BK - 1) / DG_BK;
+  if (P != nullptr) {
+    kb0 += blockIdx.z * kb_split;
+    kb1 = min(kb1, kb0 + kb_split);
+  }
   const int nkb = kb1 > kb0 ? kb1 - kb0 : 0;
 
   const uint32_t raw = smem_u32(dg_smem_raw);
@@ -215,24 +218,24 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
   const uint32_t tmem = *tslot;
 
   const size_t slabA = (size_t)Mp * Kp, slabB = (size_t)Np * Kp;
-  // 8 A slabs x 128 rows x 8 chunks of 16 B, then 8 B slabs x 64 rows x 8 chunks: 48 per thread
+  // Each thread copies the 16-byte chunk (t & 7) of rows t/8 + 32 j of every slab: 8 A slabs x 4 rows
+  // and 8 B slabs x 2 rows, 48 copies. Within a swizzle atom of 8 rows the chunk index is XORed with
+  // row & 7, which is (t / 8) & 7 for all rows of the thread.
+  const int trow = t >> 3, tch = t & 7;
+  const uint32_t sdst = base + trow * 128 + ((tch ^ (trow & 7)) << 4);
+  const __nv_bfloat16 *ga = PA + (size_t)(i0 + trow) * Kp + tch * 8;
+  const __nv_bfloat16 *gb = PB + (size_t)(j0 + trow) * Kp + tch * 8;
+  const size_t row32 = (size_t)32 * Kp;
   auto prefetch = [&](int kb) {
+    const __nv_bfloat16 *pa = ga + (size_t)kb * DG_BK, *pb = gb + (size_t)kb * DG_BK;
 #pragma unroll
-    for (int q = 0; q < 48; ++q) {
-      const int c = t + q * DG_THREADS;
-      const __nv_bfloat16 *g;
-      uint32_t dst;
-      if (q < 32) {
-        const int sl = c >> 10, r = (c >> 3) & 127, ch = c & 7;
-        g = PA + (size_t)sl * slabA + (size_t)(i0 + r) * Kp + (size_t)kb * DG_BK + ch * 8;
-        dst = base + sl * DG_ATILE + r * 128 + ((ch ^ (r & 7)) << 4);
-      } else {
-        const int cb = c - 8192;
-        const int sl = cb >> 9, r = (cb >> 3) & 63, ch = cb & 7;
-        g = PB + (size_t)sl * slabB + (size_t)(j0 + r) * Kp + (size_t)kb * DG_BK + ch * 8;
-        dst = base + DG_S * DG_ATILE + sl * DG_BTILE + r * 128 + ((ch ^ (r & 7)) << 4);
-      }
-      cp_async16(dst, g);
+    for (int sl = 0; sl < DG_S; ++sl) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) cp_async16(sdst + sl * DG_ATILE + j * 4096, pa + j * row32);
+#pragma unroll
+      for (int j = 0; j < 2; ++j) cp_async16(sdst + DG_S * DG_ATILE + sl * DG_BTILE + j * 4096, pb + j * row32);
+      pa += slabA;
+      pb += slabB;
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
@@ -248,15 +251,17 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
     __syncthreads();
     if (t == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // descriptors of the stage's first A and B slabs; the others differ only in the start address
+      // field (address / 16, no carry out of its 14 bits below 256 KB of shared memory)
+      const uint64_t da0 = tc_sdesc(base), db0 = tc_sdesc(base + DG_S * DG_ATILE);
 #pragma unroll
       for (int g = 0; g < DG_S; ++g)
 #pragma unroll
         for (int s = 0; s <= g; ++s)
 #pragma unroll
           for (int kk = 0; kk < DG_BK / 16; ++kk)
-            tc_mma(tmem + (uint32_t)(g * DG_BN), tc_sdesc(base + s * DG_ATILE + kk * 32),
-                   tc_sdesc(base + DG_S * DG_ATILE + (g - s) * DG_BTILE + kk * 32), dg_idesc(),
-                   (s | kk) != 0 ? 1u : 0u);
+            tc_mma(tmem + (uint32_t)(g * DG_BN), da0 + (uint64_t)((s * DG_ATILE + kk * 32) >> 4),
+                   db0 + (uint64_t)(((g - s) * DG_BTILE + kk * 32) >> 4), dg_idesc(), (s | kk) != 0 ? 1u : 0u);
       tc_commit(smem_u32(mbar));
       if (!mbar_wait(smem_u32(mbar), (uint32_t)(it & 1))) *sfail = 1;
     }
@@ -264,17 +269,27 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
     if (*sfail) break;
     if (it + 1 < nkb) prefetch(kb0 + it + 1);   // shared memory is free once the MMAs completed
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // groups in pairs (g, g + 1): p = 2^7 G_g + G_{g+1} fits int32 (|p| < 2^28.1) and enters the
+    // int64 with the weight of g + 1; the magic-number offsets of both raw words cancel in one add
+    const uint32_t tlane = tmem + ((uint32_t)(quad * 32) << 16);
 #pragma unroll
-    for (int g = 0; g < DG_S; ++g) {
-      uint32_t v[32];
-      tc_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(g * DG_BN + half * 32), v);
-      const int sh = 7 * (DG_S - 1 - g) - R;
-      if (sh >= 0) {
+    for (int h = 0; h < 2; ++h) {
 #pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] += (long long)dg_exact_int(v[c]) << sh;
-      } else {
+      for (int g = 0; g < DG_S; g += 2) {
+        uint32_t va[16], vb[16];
+        tc_ld16(tlane + (uint32_t)(g * DG_BN + half * 32 + h * 16), va);
+        tc_ld16(tlane + (uint32_t)((g + 1) * DG_BN + half * 32 + h * 16), vb);
+        tc_wait_ld2x16(va, vb);
+        const int sh = 7 * (DG_S - 2 - g) - R;
 #pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] += (long long)((dg_exact_int(v[c]) + (1 << (-sh - 1))) >> (-sh));
+        for (int c = 0; c < 16; ++c) {
+          const uint32_t ba = (uint32_t)__float_as_int(__uint_as_float(va[c]) + 12582912.0f);
+          const uint32_t bb = (uint32_t)__float_as_int(__uint_as_float(vb[c]) + 12582912.0f);
+          const int p = (int)((ba << 7) + bb - 0x4B400000u * 129u);
+          long long &a = acc[h * 16 + c];
+          if (sh >= 0) a += (long long)p << sh;
+          else a += (long long)((p + (1 << (-sh - 1))) >> (-sh));
+        }
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -283,7 +298,12 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
   __syncthreads();
   const bool failed = *sfail != 0;
   if (failed && t == 0) mbar_wait(smem_u32(mbar), (uint32_t)((nkb - 1) & 1));   // let in-flight MMAs drain
-  if (!failed) {
+  if (!failed && P != nullptr) {
+    long long *Pz = P + (size_t)blockIdx.z * Mp * Np;
+    const int row = i0 + quad * 32 + lane;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) Pz[row + (size_t)(j0 + half * 32 + c) * Mp] = acc[c];
+  } else if (!failed) {
     const int row = i0 + quad * 32 + lane;
     if (row < m) {
       const unsigned long long ma = rmaxA[row];
@@ -313,6 +333,27 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
   if (t == 0 && failed) atomicExch(err, 1);
 }
 
+// C = alpha 2^(EA_i + EB_j - 61 + R) sum_z P[z] + beta C over the elements a split-K product computed
+// (integer sums: the result does not depend on the split).
+__global__ void dg_splitk_reduce(int m, int n, int Mp, int Np, int splits, const long long *__restrict__ P,
+                                 const unsigned long long *rmaxA, const unsigned long long *rmaxB, int R,
+                                 double alpha, double beta, double *C, int ldc, int lowerC) {
+  const size_t total = (size_t)m * n;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const int row = (int)(idx % m), col = (int)(idx / m);
+    if (lowerC && row < col) continue;
+    long long v = 0;
+    for (int z = 0; z < splits; ++z) v += P[(size_t)z * Mp * Np + row + (size_t)col * Mp];
+    const unsigned long long ma = rmaxA[row], mb = rmaxB[col];
+    double x = ldexp((double)v, dg_row_exp(ma) + dg_row_exp(mb) - 61 + R);
+    if ((ma >> 52) >= 2047ull || (mb >> 52) >= 2047ull) x = __longlong_as_double(0x7FF8000000000000ll);
+    x *= alpha;
+    double *cp = C + row + (size_t)col * ldc;
+    if (beta != 0.0) x = fma(beta, *cp, x);
+    *cp = x;
+  }
+}
+
 // ------------------------------------------------------------------------------ host side
 bool g_tc_dgemm = false;          // gemm<double> routes here while set (the mixed form's FP64 iterations)
 bool g_tc_dgemm_mixed = true;     // dftbgpu_set_fp64_emulation
@@ -321,6 +362,9 @@ static size_t g_dg_ws_elems = 0;
 static unsigned long long *g_dg_rmax = nullptr;
 static size_t g_dg_rmax_elems = 0;
 static int *g_dg_err = nullptr;
+static long long *g_dg_part = nullptr;
+static size_t g_dg_part_elems = 0;
+constexpr int kDgSMs = 148;   // CTAs in flight (one per SM; GB300 has 152, a few may be taken)
 
 static int dg_round_up(int x, int q) { return (x + q - 1) / q * q; }
 
@@ -352,6 +396,26 @@ static int dg_ensure(size_t ws_elems, size_t rmax_elems) {
   return 0;
 }
 
+// K-splits for a product with few output tiles: enough CTAs to fill the GPU, at least four K-blocks
+// per split, at most 16 splits.
+static int dg_splits(int m, int n, int k) {
+  const long long tiles = (long long)ceil_div(m, DG_BM) * ceil_div(n, DG_BN);
+  const int nkb = ceil_div(std::max(k, 1), DG_BK);
+  if (tiles >= kDgSMs || nkb < 8) return 1;
+  long long sp = (kDgSMs + tiles - 1) / tiles;
+  sp = std::min<long long>(sp, nkb / 4);
+  sp = std::min<long long>(sp, 16);
+  return (int)std::max<long long>(sp, 1);
+}
+
+double tc_dgemm_estimate_s(int m, int n, int k) {
+  const int sp = dg_splits(m, n, k);
+  const double tiles = (double)ceil_div(m, DG_BM) * ceil_div(n, DG_BN) * sp;
+  const double waves = std::ceil(tiles / kDgSMs);
+  const double kb = std::ceil((double)ceil_div(std::max(k, 1), DG_BK) / sp);
+  return waves * kb * 5e-6 + (sp > 1 ? 20e-6 : 15e-6);
+}
+
 int tc_dgemm_reserve(int m, int n, int k) {
   const size_t Mp = (size_t)dg_round_up(m, DG_BM), Np = (size_t)dg_round_up(n, DG_BN),
                Kp = (size_t)dg_round_up(std::max(k, 1), DG_BK);
@@ -376,9 +440,32 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
   dg_pack_kernel<<<Np / 32, 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
   int R = 0;
   while ((1 << (R + 1)) < Kp) ++R;   // R = ceil(log2 Kp) - 1
-  dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN), DG_THREADS, DG_SMEM, s>>>(m, n, Kp, Mp, Np, PA, PB, rA, rB, R,
-                                                                           alpha, beta, C, ldc, flags, g_dg_err);
+  const int splits = dg_splits(m, n, k);
+  long long *Pp = nullptr;
+  int kb_split = 0;
+  if (splits > 1) {
+    const size_t need = (size_t)splits * Mp * Np;
+    if (need > g_dg_part_elems) {
+      cudaDeviceSynchronize();
+      if (g_dg_part) cudaFree(g_dg_part);
+      g_dg_part = nullptr;
+      g_dg_part_elems = 0;
+      cudaError_t e = cudaMalloc((void **)&g_dg_part, need * sizeof(long long));
+      if (e != cudaSuccess) return (int)e;
+      g_dg_part_elems = need;
+    }
+    Pp = g_dg_part;
+    kb_split = ceil_div(Kp / DG_BK, splits);
+  }
+  dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG_SMEM, s>>>(
+      m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, g_dg_err, Pp, kb_split);
   count_launch(3);
+  if (Pp) {
+    const int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
+    dg_splitk_reduce<<<rb, 256, 0, s>>>(m, n, Mp, Np, splits, Pp, rA, rB, R, alpha, beta, C, ldc,
+                                        (flags & kCLower) ? 1 : 0);
+    count_launch();
+  }
   return (int)cudaGetLastError();
 }
 

@@ -2,10 +2,11 @@
 
 The kernel splits every element of op(A) (op(B)) into eight signed 7-bit digits at a power-of-two
 scale per row (column), sums the digit products with s + t = g per 64-wide K block (exact in FP32
-because each block sum stays below 2^21), and accumulates the blocks into one int64 per output with
-weights 2^(7(7-g) - R). This model follows the same steps element by element and checks the bounds the
-kernel relies on (digit range, block sums < 2^21, int64 range) and the error bound stated in the kernel
-against exact rational arithmetic."""
+because each block sum stays below 2^21), combines the block sums in pairs 2^7 G_g + G_{g+1} (int32)
+and accumulates them into one int64 per output with weights 2^(7(6-g) - R). This model follows the
+same steps element by element and checks the bounds the kernel relies on (digit range, block sums
+< 2^21, pair sums in int32, int64 range) and the error bound stated in the kernel against exact
+rational arithmetic."""
 import struct
 from fractions import Fraction
 
@@ -72,12 +73,15 @@ def model_gemm(A, B):
         for j in range(n):
             acc = 0
             for k0 in range(0, K, BK):
-                for g in range(S):
-                    G = sum(da[i][k][s] * db[j][k][g - s] for k in range(k0, min(K, k0 + BK)) for s in range(g + 1))
-                    assert abs(G) <= 2 ** 21          # exact in the FP32 tensor-memory accumulator
-                    sh = 7 * (S - 1 - g) - R
-                    acc += G << sh if sh >= 0 else (G + (1 << (-sh - 1))) >> (-sh)
-                    assert abs(acc) < 2 ** 63          # int64 accumulator
+                G = [sum(da[i][k][s] * db[j][k][g - s] for k in range(k0, min(K, k0 + BK)) for s in range(g + 1))
+                     for g in range(S)]
+                assert max(abs(x) for x in G) <= 2 ** 21      # exact in the FP32 tensor-memory accumulator
+                for g in range(0, S, 2):                       # read back in pairs (g, g + 1)
+                    p = (G[g] << 7) + G[g + 1]
+                    assert abs(p) < 2 ** 31                    # int32
+                    sh = 7 * (S - 2 - g) - R
+                    acc += p << sh if sh >= 0 else (p + (1 << (-sh - 1))) >> (-sh)
+                    assert abs(acc) < 2 ** 63                  # int64 accumulator
             C[i, j] = float(Fraction(acc) * Fraction(2) ** (EA[i] + EB[j] - 61 + R))
     return C
 

@@ -72,6 +72,8 @@ def _dref(ta, tb, A, B):
     (384, 257, 640, "T", "N"),
     (129, 511, 77, "T", "T"),
     (96, 40, 32, "N", "N"),        # smaller than one tile
+    (64, 64, 2000, "T", "N"),      # one tile, long K: split over 8 CTAs along K
+    (64, 512, 1500, "T", "N"),     # few tiles: split along K
 ])
 def test_tc_dgemm_products(gpu_lib, m, n, k, ta, tb):
     from dftbplus_gb300 import binding
@@ -106,6 +108,31 @@ def test_tc_dgemm_scales_zeros_and_flags(gpu_lib):
     assert np.all(np.abs(C - ref)[low] <= tol[low]), np.max((np.abs(C - ref) / tol)[low])
     assert np.array_equal(C[~low], C0[~low])
     assert np.array_equal(C[17, :18], C0[17, :18])          # zero row: alpha * 0 + beta * C0
+    ctx.close()
+
+
+def test_tc_dgemm_split_lower_beta(gpu_lib):
+    """Split-K with a lower-only output and beta accumulation (int64 partials summed exactly): the
+    same product split and unsplit agree bit for bit."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(21)
+    m, k = 256, 1200                 # 4 x 4 tiles (lower half computed), 19 K blocks: split 4 ways
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, m))
+    C0 = rng.standard_normal((m, m))
+    ctx = binding.Context(0)
+    kCLower = 16
+    C = ctx.test_dgemm_tc("N", "N", A, B, C=C0, alpha=-1.0, beta=1.0, flags=kCLower)
+    ref, tol = _dref("N", "N", A, B)
+    ref = C0 - ref
+    tol = tol + 2.0 ** -52 * np.abs(C0)
+    low = np.tril(np.ones((m, m), dtype=bool))
+    assert np.all(np.abs(C - ref)[low] <= tol[low])
+    assert np.array_equal(C[~low], C0[~low])
+    # the same product computed as two K halves added by beta reproduces the result to rounding
+    C2 = ctx.test_dgemm_tc("N", "N", A[:, :600], B[:600], C=C0, alpha=-1.0, beta=1.0, flags=kCLower)
+    C2 = ctx.test_dgemm_tc("N", "N", A[:, 600:], B[600:], C=C2, alpha=-1.0, beta=1.0, flags=kCLower)
+    assert np.all(np.abs(C2 - C)[low] <= 2 * tol[low])
     ctx.close()
 
 
