@@ -578,7 +578,7 @@ def run_gpu(args):
                         "fp64_equivalent_tflops": (v["flops"] / (v["ms"] / 1e3) / 1e12) if v["ms"] > 0 else None}
                     for k, v in classes.items()}
     kernels = {"fp64": "dgemm_kernel<double> (all FP64 GEMM launches)",
-               "fp32": "dgemm_kernel<float> (FP32 GEMM launches)",
+               "fp32": "dgemm_kernel<float> and sgemm128_kernel (FP32 FMA GEMM launches)",
                "tc_fp64": "dg_gemm_kernel (FP64 products as 36 exact BF16 digit products on tcgen05, "
                           "with their two packing launches)"}
     peak_src = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 entry in the measured peaks)",

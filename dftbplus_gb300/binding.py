@@ -74,6 +74,9 @@ SIGNATURES = {
                                      _dp, _dp, C.c_double, _dp, C.c_int]),
     "dftbgpu_set_tensor_cores": (C.c_int, [C.c_int]),
     "dftbgpu_set_fp64_emulation": (C.c_int, [C.c_int]),
+    "dftbgpu_test_sgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
+                                     C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
+                                     C.POINTER(C.c_float), C.c_int, C.c_int]),
     "dftbgpu_test_dgemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_double,
                                         _dp, C.c_int, _dp, C.c_int, C.c_double, _dp, C.c_int, C.c_int]),
     "dftbgpu_test_gemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
@@ -293,6 +296,19 @@ class Context:
         self.check(self.lib.dftbgpu_test_gemm_tc(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
                                                  _p(A, C_float), A.shape[0], _p(B, C_float), B.shape[0], beta,
                                                  _p(Cm, C_float), m, flags))
+        return Cm
+
+    def test_sgemm(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):
+        """C = alpha op(A) op(B) + beta C with the library's FP32 FMA GEMM (float32, column-major)."""
+        A = np.asfortranarray(A, dtype=np.float32)
+        B = np.asfortranarray(B, dtype=np.float32)
+        m = A.shape[1] if ta == "T" else A.shape[0]
+        k = A.shape[0] if ta == "T" else A.shape[1]
+        n = B.shape[0] if tb == "T" else B.shape[1]
+        Cm = np.zeros((m, n), dtype=np.float32, order="F") if C is None else np.array(C, dtype=np.float32, order="F")
+        self.check(self.lib.dftbgpu_test_sgemm(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
+                                               _p(A, C_float), A.shape[0], _p(B, C_float), B.shape[0], beta,
+                                               _p(Cm, C_float), m, flags))
         return Cm
 
     def test_dgemm_tc(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):

@@ -1115,6 +1115,29 @@ int dftbgpu_sygvd(dftbgpu_ctx *c, int n, double *a, double *b, double *w) {
 
 extern "C" {
 
+int dftbgpu_test_sgemm(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, float alpha, const float *a, int lda,
+                       const float *b, int ldb, float beta, float *cm, int ldc, int flags) {
+  if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  const size_t na = (size_t)lda * ((ta == 'N') ? k : m), nb = (size_t)ldb * ((tb == 'N') ? n : k),
+               nc = (size_t)ldc * n;
+  float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  DG_CUDA(c, cudaMalloc((void **)&dA, na * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dB, nb * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dC, nc * sizeof(float)));
+  DG_CUDA(c, cudaMemcpy(dA, a, na * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dB, b, nb * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dC, cm, nc * sizeof(float), cudaMemcpyHostToDevice));
+  dg::gemm<float>(c->stream, ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, flags);
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  DG_CUDA(c, cudaGetLastError());
+  DG_CUDA(c, cudaMemcpy(cm, dC, nc * sizeof(float), cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  return DFTBGPU_OK;
+}
+
 int dftbgpu_test_dgemm(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                        const double *b, double beta, double *cm, int flags) {
   if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k < 0) return DFTBGPU_ERR_ARGS;

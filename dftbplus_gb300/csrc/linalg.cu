@@ -160,6 +160,122 @@ __global__ void dgemm_splitk_reduce(int m, int n, int splits, const T *__restric
   }
 }
 
+// FP32 GEMM for products with many output tiles: 128 x 128 tile per CTA, 256 threads, 8 x 8 outputs
+// per thread (rows tx*4 + {0..3} and 64 + tx*4 + {0..3}, columns likewise from ty, so that shared
+// memory is read as float4 without bank conflicts), K step 16 with register prefetch of the next
+// slab. Shared rows are padded to 132 floats so that the transposed stores of either operand layout
+// are conflict-free. Same flags as dgemm_kernel; with kCLower only elements on or below the diagonal
+// are written. No split-K (it is used only where the tiles fill the GPU). Two CTAs per SM (128
+// registers per thread).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256, 2) sgemm128_kernel(int m, int n, int k, float alpha,
+                                                      const float *__restrict__ A, int lda,
+                                                      const float *__restrict__ B, int ldb, float beta,
+                                                      float *__restrict__ C, int ldc, int flags) {
+  constexpr int BM = 128, BN = 128, BK = 16, LDS = 132;
+  __shared__ __align__(16) float As[BK][LDS];
+  __shared__ __align__(16) float Bs[BK][LDS];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int i0 = blockIdx.x * BM, j0 = blockIdx.y * BN;
+  if ((flags & kCLower) && i0 + BM - 1 < j0) return;
+  int kmin = 0, kmax = k;
+  if (flags & kALower) kmax = min(kmax, i0 + BM);
+  if (flags & kAUpper) kmin = max(kmin, i0);
+  if (flags & kBLower) kmin = max(kmin, j0);
+  if (flags & kBUpper) kmax = min(kmax, j0 + BN);
+
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  float ra[8], rb[8];
+  // element q of this thread's share of a 128 x 16 slab: (row, kk) with the contiguous source index
+  // running fastest across threads
+  auto load_a = [&](int p0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int t = tid + 256 * q;
+      int ii, pp;
+      if (!TA) { ii = t & 127; pp = t >> 7; } else { pp = t & 15; ii = t >> 4; }
+      const int gi = i0 + ii, gp = p0 + pp;
+      float v = 0.f;
+      if (gi < m && gp < kmax) v = TA ? A[gp + (size_t)gi * lda] : A[gi + (size_t)gp * lda];
+      ra[q] = v;
+    }
+  };
+  auto load_b = [&](int p0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int t = tid + 256 * q;
+      int jj, pp;
+      if (TB) { jj = t & 127; pp = t >> 7; } else { pp = t & 15; jj = t >> 4; }
+      const int gj = j0 + jj, gp = p0 + pp;
+      float v = 0.f;
+      if (gj < n && gp < kmax) v = TB ? B[gj + (size_t)gp * ldb] : B[gp + (size_t)gj * ldb];
+      rb[q] = v;
+    }
+  };
+  auto store_ab = [&]() {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int t = tid + 256 * q;
+      int ii, pp;
+      if (!TA) { ii = t & 127; pp = t >> 7; } else { pp = t & 15; ii = t >> 4; }
+      As[pp][ii] = ra[q];
+      int jj, qq;
+      if (TB) { jj = t & 127; qq = t >> 7; } else { qq = t & 15; jj = t >> 4; }
+      Bs[qq][jj] = rb[q];
+    }
+  };
+
+  if (kmin < kmax) {
+    load_a(kmin);
+    load_b(kmin);
+    for (int p0 = kmin; p0 < kmax; p0 += BK) {
+      __syncthreads();
+      store_ab();
+      __syncthreads();
+      if (p0 + BK < kmax) {
+        load_a(p0 + BK);
+        load_b(p0 + BK);
+      }
+#pragma unroll
+      for (int pp = 0; pp < BK; ++pp) {
+        const float4 a0 = *reinterpret_cast<const float4 *>(&As[pp][tx * 4]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&As[pp][64 + tx * 4]);
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[pp][ty * 4]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[pp][64 + ty * 4]);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+      }
+    }
+  }
+  const bool lower = (flags & kCLower) != 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int gj = j0 + (j < 4 ? ty * 4 + j : 64 + ty * 4 + (j - 4));
+    if (gj >= n) continue;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int gi = i0 + (i < 4 ? tx * 4 + i : 64 + tx * 4 + (i - 4));
+      if (gi >= m || (lower && gi < gj)) continue;
+      float *c = C + gi + (size_t)gj * ldc;
+      float v = alpha * acc[i][j];
+      if (beta != 0.f) v = fmaf(beta, *c, v);
+      *c = v;
+    }
+  }
+}
+
+bool g_sgemm128 = true;   // FP32 products with many tiles on sgemm128_kernel
+
 GemmProfile g_gemm_prof;
 
 static double gemm_executed_flops(int m, int n, int k, int flags) {
@@ -212,11 +328,29 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
   }
   T *P = (splits > 1) ? work : nullptr;
   grid.z = splits;
-  bool done = false;
+  bool done = false, on_tc = false;
   if constexpr (std::is_same<T, double>::value) {
     if (g_tc_dgemm && m >= 64 && n >= 64 && k >= 32 && cap == cudaStreamCaptureStatusNone &&
         tc_dgemm_faster(m, n, k)) {
       tc_dgemm(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      done = true;
+      on_tc = true;
+      P = nullptr;
+    }
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    const long long tiles128 = (long long)ceil_div(m, 128) * ceil_div(n, 128);
+    if (g_sgemm128 && tiles128 >= 2 * 152) {
+      const dim3 g128(ceil_div(m, 128), ceil_div(n, 128));
+      if (!TA && !TB)
+        sgemm128_kernel<false, false><<<g128, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      else if (!TA && TB)
+        sgemm128_kernel<false, true><<<g128, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      else if (TA && !TB)
+        sgemm128_kernel<true, false><<<g128, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      else
+        sgemm128_kernel<true, true><<<g128, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
+      count_launch();
       done = true;
       P = nullptr;
     }
@@ -241,7 +375,7 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
     g_gemm_prof.ev.push_back(e0);
     g_gemm_prof.ev.push_back(e1);
     g_gemm_prof.flops.push_back(gemm_executed_flops(m, n, k, flags));
-    g_gemm_prof.phase.push_back(done ? kPhGemmTc : (sizeof(T) == 4 ? kPhGemm32 : kPhGemm));
+    g_gemm_prof.phase.push_back(on_tc ? kPhGemmTc : (sizeof(T) == 4 ? kPhGemm32 : kPhGemm));
   }
 }
 

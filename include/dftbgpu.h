@@ -263,6 +263,10 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k
 int dftbgpu_set_fp64_emulation(int enable);
 int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                           int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
+/* FP32 product of the mixed form's FP32 iterations (FP32 FMA; 128 x 128 tiles where they fill the GPU),
+ * host arrays as dftbgpu_test_gemm_tc (no reference counterpart; a test hook). */
+int dftbgpu_test_sgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha, const float *a,
+                       int lda, const float *b, int ldb, float beta, float *c, int ldc, int flags);
 int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
                        const double *a, const double *b, double beta, double *c, int flags);
 int dftbgpu_test_tridiag(dftbgpu_ctx *ctx, int n, const double *a, double *d, double *e);

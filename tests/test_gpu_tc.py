@@ -150,3 +150,40 @@ def test_tc_dgemm_largest_digit_sums(gpu_lib):
     exact = -k * x * x
     assert np.all(np.abs(C - exact) <= abs(exact) * 2.0 ** -50)
     ctx.close()
+
+
+# ------------------------------------------------------------------ FP32 FMA products (128 x 128 tiles)
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_sgemm_large_tiles(gpu_lib, ta, tb):
+    """Products with enough 128 x 128 tiles to fill the GPU take the large-tile FP32 kernel (ragged
+    edges, K not a multiple of the K step); FP32 FMA bound 1e-6 sum_k |a_ik| |b_kj|."""
+    from dftbplus_gb300 import binding
+    m, n, k = 2500, 2437, 301
+    rng = np.random.default_rng(len(ta + tb) + (ta == "T") * 3 + (tb == "T"))
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k)).astype(np.float32)
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n)).astype(np.float32)
+    ctx = binding.Context(0)
+    C = ctx.test_sgemm(ta, tb, A, B)
+    ref, mag = _ref(ta, tb, A, B)
+    assert np.all(np.abs(C - ref) <= 1e-6 * mag + 1e-6), np.max(np.abs(C - ref) / (mag + 1e-30))
+    ctx.close()
+
+
+def test_sgemm_large_tiles_flags_beta(gpu_lib):
+    """Triangular hints, lower-only output (elements above the diagonal keep their bits) and beta, as
+    the FP32 iterations use them (reduced transform, tridiagonalisation updates, density)."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(8)
+    n = 2304
+    L = np.tril(rng.standard_normal((n, n))).astype(np.float32)   # the hints promise these zeros
+    X = np.tril(rng.standard_normal((n, n))).astype(np.float32)
+    C0 = rng.standard_normal((n, n)).astype(np.float32)
+    kALower, kBLower, kCLower = 1, 4, 16
+    ctx = binding.Context(0)
+    C = ctx.test_sgemm("N", "N", L, X, C=C0, alpha=-0.5, beta=1.0, flags=kALower | kBLower | kCLower)
+    ref = -0.5 * (L.astype(np.float64) @ X) + C0
+    mag = 0.5 * (np.abs(L).astype(np.float64) @ np.abs(X)) + np.abs(C0)
+    low = np.tril(np.ones((n, n), dtype=bool))
+    assert np.all(np.abs(C - ref)[low] <= 1e-6 * mag[low] + 1e-6)
+    assert np.array_equal(C[~low], C0[~low])
+    ctx.close()
