@@ -13,7 +13,7 @@
 
 namespace dg {
 
-long long g_launches = 0;
+std::atomic<long long> g_launches{0};
 
 struct Ctx {
   int device = 0;

@@ -1,6 +1,7 @@
 // Shared definitions of the dftbgpu CUDA library (sm_103a).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -59,7 +60,7 @@ int set_error(Ctx *c, int code, const char *fmt, ...);
   } while (0)
 
 // Count of kernel launches issued by this library (for launch accounting).
-extern long long g_launches;
+extern std::atomic<long long> g_launches;
 inline void count_launch(long long n = 1) { g_launches += n; }
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }

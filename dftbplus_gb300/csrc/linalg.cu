@@ -274,9 +274,9 @@ __global__ void __launch_bounds__(256, 2) sgemm128_kernel(int m, int n, int k, f
   }
 }
 
-bool g_sgemm128 = true;   // FP32 products with many tiles on sgemm128_kernel
+std::atomic<bool> g_sgemm128{true};   // FP32 products with many tiles on sgemm128_kernel
 
-GemmProfile g_gemm_prof;
+thread_local GemmProfile g_gemm_prof;
 
 static double gemm_executed_flops(int m, int n, int k, int flags) {
   double f = 0.0;

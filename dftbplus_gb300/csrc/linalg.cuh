@@ -2,6 +2,8 @@
 // pieces are templates on the scalar type: FP64 for the plain path, FP32 for the reduced-precision
 // SCC iterations of the mixed form. Cholesky and L^-1 are FP64 only.
 #pragma once
+#include <atomic>
+
 #include "common.cuh"
 
 namespace dg {
@@ -31,7 +33,7 @@ int tc_gemm_error();
 // When set, the perturbative updates of the mixed form use tc_gemm. Their operands carry the
 // potential change only, so the tensor cores' accumulation (not IEEE round-to-nearest over long K)
 // is scaled down by it; full FP32 eigensolves keep FP32 FMA products.
-extern bool g_tc_gemm;
+extern std::atomic<bool> g_tc_gemm;   // process-wide switch
 
 // FP64-class product on the tensor cores (tc_dgemm.cu): exact BF16 digit-slice products (eight
 // 7-bit digits per element, integer accumulation), same arguments and flags as gemm. Returns a
@@ -44,8 +46,8 @@ int tc_dgemm_error();
 // While g_tc_dgemm is set, gemm<double> sends products with m, n >= 64 and k >= 32 to tc_dgemm
 // where a cost estimate favours it (the mixed form sets it around its FP64 iterations when
 // g_tc_dgemm_mixed allows it).
-extern bool g_tc_dgemm;
-extern bool g_tc_dgemm_mixed;
+extern thread_local bool g_tc_dgemm;        // per calling thread
+extern std::atomic<bool> g_tc_dgemm_mixed;  // process-wide switch
 
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
@@ -61,7 +63,7 @@ struct GemmProfile {
   std::vector<int> phase;          // per pair: kPhGemm (FP64), kPhGemm32 (FP32) or kPhGemmTc
                                    // (FP64 as tensor-core digit-slice products)
 };
-extern GemmProfile g_gemm_prof;
+extern thread_local GemmProfile g_gemm_prof;   // per calling thread (its context's profiler)
 
 // In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
 void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);

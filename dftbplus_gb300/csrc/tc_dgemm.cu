@@ -36,9 +36,11 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "linalg.cuh"
+#include "scratch.cuh"
 #include "tcgen05.cuh"
 
 namespace dg {
@@ -355,45 +357,23 @@ __global__ void dg_splitk_reduce(int m, int n, int Mp, int Np, int splits, const
 }
 
 // ------------------------------------------------------------------------------ host side
-bool g_tc_dgemm = false;          // gemm<double> routes here while set (the mixed form's FP64 iterations)
-bool g_tc_dgemm_mixed = true;     // dftbgpu_set_fp64_emulation
-static __nv_bfloat16 *g_dg_ws = nullptr;
-static size_t g_dg_ws_elems = 0;
-static unsigned long long *g_dg_rmax = nullptr;
-static size_t g_dg_rmax_elems = 0;
-static int *g_dg_err = nullptr;
-static long long *g_dg_part = nullptr;
-static size_t g_dg_part_elems = 0;
+thread_local bool g_tc_dgemm = false;   // gemm<double> routes here while set (calling thread only)
+std::atomic<bool> g_tc_dgemm_mixed{true};   // dftbgpu_set_fp64_emulation
 constexpr int kDgSMs = 148;   // CTAs in flight (one per SM; GB300 has 152, a few may be taken)
+// scratch of this thread on the current device: digit slabs, row maxima, split-K partials
+static thread_local ThreadScratch t_dg;
+enum { kDgSlabs = 0, kDgRmax = 1, kDgPart = 2 };
 
 static int dg_round_up(int x, int q) { return (x + q - 1) / q * q; }
 
-static int dg_ensure(size_t ws_elems, size_t rmax_elems) {
-  if (ws_elems > g_dg_ws_elems) {
-    cudaDeviceSynchronize();
-    if (g_dg_ws) cudaFree(g_dg_ws);
-    g_dg_ws = nullptr;
-    g_dg_ws_elems = 0;
-    cudaError_t e = cudaMalloc((void **)&g_dg_ws, ws_elems * sizeof(__nv_bfloat16));
-    if (e != cudaSuccess) return (int)e;
-    g_dg_ws_elems = ws_elems;
+static int dg_ensure(DeviceScratch &d, size_t ws_elems, size_t rmax_elems) {
+  int rc = scratch_reserve(d.buf[kDgSlabs], ws_elems * sizeof(__nv_bfloat16));
+  if (rc == 0) rc = scratch_reserve(d.buf[kDgRmax], rmax_elems * sizeof(unsigned long long));
+  if (rc == 0 && !d.err) {
+    rc = scratch_err(d);
+    if (rc == 0) rc = (int)cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM);
   }
-  if (rmax_elems > g_dg_rmax_elems) {
-    cudaDeviceSynchronize();
-    if (g_dg_rmax) cudaFree(g_dg_rmax);
-    g_dg_rmax = nullptr;
-    g_dg_rmax_elems = 0;
-    cudaError_t e = cudaMalloc((void **)&g_dg_rmax, rmax_elems * sizeof(unsigned long long));
-    if (e != cudaSuccess) return (int)e;
-    g_dg_rmax_elems = rmax_elems;
-  }
-  if (!g_dg_err) {
-    cudaError_t e = cudaMalloc((void **)&g_dg_err, sizeof(int));
-    if (e != cudaSuccess) return (int)e;
-    cudaMemset(g_dg_err, 0, sizeof(int));
-    cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM);
-  }
-  return 0;
+  return rc;
 }
 
 // K-splits for a product with few output tiles: enough CTAs to fill the GPU, at least four K-blocks
@@ -419,17 +399,18 @@ double tc_dgemm_estimate_s(int m, int n, int k) {
 int tc_dgemm_reserve(int m, int n, int k) {
   const size_t Mp = (size_t)dg_round_up(m, DG_BM), Np = (size_t)dg_round_up(n, DG_BN),
                Kp = (size_t)dg_round_up(std::max(k, 1), DG_BK);
-  return dg_ensure((size_t)DG_S * (Mp + Np) * Kp, Mp + Np);
+  return dg_ensure(t_dg.current(), (size_t)DG_S * (Mp + Np) * Kp, Mp + Np);
 }
 
 int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
              const double *B, int ldb, double beta, double *C, int ldc, int flags) {
   if (m <= 0 || n <= 0) return 0;
   const int Mp = dg_round_up(m, DG_BM), Np = dg_round_up(n, DG_BN), Kp = dg_round_up(std::max(k, 1), DG_BK);
-  int rc = dg_ensure((size_t)DG_S * ((size_t)Mp + (size_t)Np) * Kp, (size_t)Mp + Np);
+  DeviceScratch &ds = t_dg.current();
+  int rc = dg_ensure(ds, (size_t)DG_S * ((size_t)Mp + (size_t)Np) * Kp, (size_t)Mp + Np);
   if (rc != 0) return rc;
-  __nv_bfloat16 *PA = g_dg_ws, *PB = PA + (size_t)DG_S * Mp * Kp;
-  unsigned long long *rA = g_dg_rmax, *rB = g_dg_rmax + Mp;
+  __nv_bfloat16 *PA = static_cast<__nv_bfloat16 *>(ds.buf[kDgSlabs].p), *PB = PA + (size_t)DG_S * Mp * Kp;
+  unsigned long long *rA = static_cast<unsigned long long *>(ds.buf[kDgRmax].p), *rB = rA + Mp;
   const bool TA = (ta == 'T' || ta == 't'), TB = (tb == 'T' || tb == 't');
   // op(A)(r, k) and op(B)^T(j, k) as strided views; structural zeros from the triangular flags
   const long long ars = TA ? lda : 1, aks = TA ? 1 : lda;
@@ -444,21 +425,13 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
   long long *Pp = nullptr;
   int kb_split = 0;
   if (splits > 1) {
-    const size_t need = (size_t)splits * Mp * Np;
-    if (need > g_dg_part_elems) {
-      cudaDeviceSynchronize();
-      if (g_dg_part) cudaFree(g_dg_part);
-      g_dg_part = nullptr;
-      g_dg_part_elems = 0;
-      cudaError_t e = cudaMalloc((void **)&g_dg_part, need * sizeof(long long));
-      if (e != cudaSuccess) return (int)e;
-      g_dg_part_elems = need;
-    }
-    Pp = g_dg_part;
+    rc = scratch_reserve(ds.buf[kDgPart], (size_t)splits * Mp * Np * sizeof(long long));
+    if (rc != 0) return rc;
+    Pp = static_cast<long long *>(ds.buf[kDgPart].p);
     kb_split = ceil_div(Kp / DG_BK, splits);
   }
   dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG_SMEM, s>>>(
-      m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, g_dg_err, Pp, kb_split);
+      m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
   count_launch(3);
   if (Pp) {
     const int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
@@ -469,12 +442,6 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
   return (int)cudaGetLastError();
 }
 
-int tc_dgemm_error() {
-  if (!g_dg_err) return 0;
-  int h = 0;
-  cudaMemcpy(&h, g_dg_err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (h) cudaMemset(g_dg_err, 0, sizeof(int));
-  return h;
-}
+int tc_dgemm_error() { return scratch_take_err(t_dg.current()); }
 
 }  // namespace dg

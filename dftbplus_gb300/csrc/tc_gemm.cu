@@ -13,7 +13,10 @@
 // tcgen05.ld. Every wait is bounded; on a timeout the kernel records an error and releases its TMEM.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "linalg.cuh"
+#include "scratch.cuh"
 #include "tcgen05.cuh"
 
 namespace dg {
@@ -171,10 +174,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(int m, int n, in
 }
 
 // ------------------------------------------------------------------------------ host side
-bool g_tc_gemm = true;    // perturbative updates on the tensor cores (dftbgpu_set_tensor_cores)
-static __nv_bfloat16 *g_tc_ws = nullptr;
-static size_t g_tc_ws_elems = 0;
-static int *g_tc_err = nullptr;
+std::atomic<bool> g_tc_gemm{true};   // perturbative updates on the tensor cores (dftbgpu_set_tensor_cores)
+static thread_local ThreadScratch t_tc;   // packed slabs of this thread on the current device
 
 static int round_up(int x, int q) { return (x + q - 1) / q * q; }
 
@@ -183,26 +184,15 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
   if (m <= 0 || n <= 0) return 0;
   const int Mp = round_up(m, TC_BM), Np = round_up(n, TC_BN), Kp = round_up(std::max(k, 1), TC_BK);
   const size_t need = (size_t)TC_SPLIT * ((size_t)Mp + (size_t)Np) * Kp;
-  if (need > g_tc_ws_elems) {
-    cudaDeviceSynchronize();
-    if (g_tc_ws) cudaFree(g_tc_ws);
-    g_tc_ws = nullptr;
-    g_tc_ws_elems = 0;
-    cudaError_t e = cudaMalloc((void **)&g_tc_ws, need * sizeof(__nv_bfloat16));
-    if (e != cudaSuccess) return (int)e;
-    g_tc_ws_elems = need;
+  DeviceScratch &ds = t_tc.current();
+  int rc = scratch_reserve(ds.buf[0], need * sizeof(__nv_bfloat16));
+  if (rc != 0) return rc;
+  if (!ds.err) {
+    rc = scratch_err(ds);
+    if (rc == 0) rc = (int)cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
+    if (rc != 0) return rc;
   }
-  if (!g_tc_err) {
-    cudaError_t e = cudaMalloc((void **)&g_tc_err, sizeof(int));
-    if (e != cudaSuccess) return (int)e;
-    cudaMemset(g_tc_err, 0, sizeof(int));
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_BYTES);
-      attr = true;
-    }
-  }
-  __nv_bfloat16 *PA = g_tc_ws, *PB = PA + (size_t)TC_SPLIT * Mp * Kp;
+  __nv_bfloat16 *PA = static_cast<__nv_bfloat16 *>(ds.buf[0].p), *PB = PA + (size_t)TC_SPLIT * Mp * Kp;
   // op(A)(r, k) and op(B)^T(j, k) as strided views; structural zeros from the triangular flags
   const long long ars = (ta == 'N') ? 1 : lda, aks = (ta == 'N') ? lda : 1;
   const long long brs = (tb == 'N') ? ldb : 1, bks = (tb == 'N') ? 1 : ldb;
@@ -221,7 +211,7 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
   tc_pack_kernel<<<dim3(Kp / 32, Mp / 32), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, PA, PA + sa, PA + 2 * sa);
   tc_pack_kernel<<<dim3(Kp / 32, Np / 32), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, PB, PB + sb, PB + 2 * sb);
   tc_gemm_kernel<<<dim3(Mp / TC_BM, Np / TC_BN), TC_THREADS, TC_SMEM_BYTES, s>>>(
-      m, n, Kp, Mp, Np, PA, PB, alpha, beta, C, ldc, (flags & kCLower) ? 1 : 0, g_tc_err);
+      m, n, Kp, Mp, Np, PA, PB, alpha, beta, C, ldc, (flags & kCLower) ? 1 : 0, ds.err);
   count_launch(3);
   if (prof) {
     cudaEventRecord(e1, s);
@@ -233,12 +223,6 @@ int tc_gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, 
   return (int)cudaGetLastError();
 }
 
-int tc_gemm_error() {
-  if (!g_tc_err) return 0;
-  int h = 0;
-  cudaMemcpy(&h, g_tc_err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (h) cudaMemset(g_tc_err, 0, sizeof(int));
-  return h;
-}
+int tc_gemm_error() { return scratch_take_err(t_tc.current()); }
 
 }  // namespace dg
