@@ -293,10 +293,9 @@ static int ensure_mixed(Ctx *c, int n) {
     c->cap_n32 = n;
     c->mixed_ready = false;
   }
-  if (g_tc_dgemm_mixed) {
-    const int e = tc_dgemm_reserve(n, n, n);
-    if (e != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tensor-core FP64 workspace: %s", cudaGetErrorString((cudaError_t)e));
-  }
+  // size the tensor-core FP64 scratch once; if the device cannot hold it, the FP64 products of the
+  // mixed form stay on FP64 FMA (gemm<double> falls back per product)
+  if (g_tc_dgemm_mixed) tc_dgemm_reserve(n, n, n);
   if (!c->mixed_ready) {
     size_t nn = (size_t)n * n;
     convert_d2f(c->stream, nn, c->Lc, c->L32);

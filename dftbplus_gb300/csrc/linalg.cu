@@ -332,10 +332,12 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
   if constexpr (std::is_same<T, double>::value) {
     if (g_tc_dgemm && m >= 64 && n >= 64 && k >= 32 && cap == cudaStreamCaptureStatusNone &&
         tc_dgemm_faster(m, n, k)) {
-      tc_dgemm(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);
-      done = true;
-      on_tc = true;
-      P = nullptr;
+      // a scratch allocation that fails leaves the product to the FP64 FMA kernel below
+      if (tc_dgemm(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags) == 0) {
+        done = true;
+        on_tc = true;
+        P = nullptr;
+      }
     }
   }
   if constexpr (std::is_same<T, float>::value) {

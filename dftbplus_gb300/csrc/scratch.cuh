@@ -57,7 +57,11 @@ inline int scratch_reserve(ScratchBuf &b, size_t bytes) {
   b.p = nullptr;
   b.bytes = 0;
   const cudaError_t e = cudaMalloc(&b.p, bytes);
-  if (e != cudaSuccess) return (int)e;
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    cudaGetLastError();   // an out-of-memory here is reported by the return value only
+    return (int)e;
+  }
   b.bytes = bytes;
   return 0;
 }
@@ -66,7 +70,11 @@ inline int scratch_reserve(ScratchBuf &b, size_t bytes) {
 inline int scratch_err(DeviceScratch &d) {
   if (d.err) return 0;
   const cudaError_t e = cudaMalloc((void **)&d.err, sizeof(int));
-  if (e != cudaSuccess) return (int)e;
+  if (e != cudaSuccess) {
+    d.err = nullptr;
+    cudaGetLastError();
+    return (int)e;
+  }
   return (int)cudaMemset(d.err, 0, sizeof(int));
 }
 
