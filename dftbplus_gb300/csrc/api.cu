@@ -924,6 +924,8 @@ static int gradients_impl(dftbgpu_ctx *c, double *grad, bool dev) {
     DG_CUDA(c, cudaMemcpyAsync(grad, c->d_grad, sizeof(double) * 3 * c->natom, cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
   }
+  if (c->scc_mixed && tc_dgemm_error())   // read after the stream synchronised
+    return set_error(c, DFTBGPU_ERR_ITER_CAP, "tensor-core GEMM: a bounded wait timed out");
   flush_marks(c);
   return DFTBGPU_OK;
 }
