@@ -109,38 +109,102 @@ def write_skf(path_or_buf, dist: float, ham10: np.ndarray, over10: np.ndarray, *
             fh.write(text)
 
 
+class _ListDirected:
+    """Fortran list-directed input (``read(unit, *)``) over the records (lines) of a file, the way
+    the reference reads every SKF data line (``type/oldskdata.F90:139-202``, ``:233-262``).
+
+    Values are separated by blanks or a comma; ``r*c`` stands for r copies of c and ``r*`` for r null
+    values; two commas with nothing between are one null value; a slash ends the read (the items
+    left keep their values). A D exponent (``1.0D-3``) reads as E. One read consumes as many records
+    as it needs and drops the rest of its last record. Null values come back as None.
+    """
+
+    def __init__(self, lines: List[str], pos: int = 0):
+        self.lines = lines
+        self.pos = pos
+
+    @staticmethod
+    def _conv(tok: str) -> float:
+        return float(tok.replace("D", "E").replace("d", "e"))
+
+    @classmethod
+    def _items(cls, line: str):
+        """Values of one record in order, converted only when taken (None for a null, '/' for a
+        slash): a read stops taking items once it has enough, so the rest of the record may hold
+        anything."""
+        fields = line.split(",")
+        for fi, field in enumerate(fields):
+            toks = field.split()
+            if not toks:
+                # ",," or a leading comma: one null value (a trailing comma adds nothing)
+                if fi < len(fields) - 1:
+                    yield None
+                continue
+            for tok in toks:
+                if tok.startswith("/"):
+                    yield "/"
+                    return
+                if "*" in tok:
+                    r, c = tok.split("*", 1)
+                    val = None if c == "" else cls._conv(c)
+                    for _ in range(int(r)):
+                        yield val
+                else:
+                    yield cls._conv(tok)
+
+    def read(self, n: int) -> List[float | None]:
+        vals: List[float | None] = []
+        while len(vals) < n:
+            if self.pos >= len(self.lines):
+                raise ValueError("SKF data ended in the middle of a list-directed read")
+            line = self.lines[self.pos]
+            self.pos += 1
+            for item in self._items(line):
+                if isinstance(item, str):       # slash: the remaining items are not read
+                    vals.extend([None] * (n - len(vals)))
+                    break
+                vals.append(item)
+                if len(vals) == n:
+                    break
+        return vals
+
+
+def _num(v, default: float = 0.0) -> float:
+    return default if v is None else float(v)
+
+
 def read_skf(path_or_text, homo: bool, read_repulsive: bool = True) -> SkfData:
-    """Parse an SKF file (10-column or '@' extended 20-column format)."""
+    """Parse an SKF file (10-column or '@' extended 20-column format) with the reference's
+    list-directed reads: dist and nGrid, the homonuclear line (nShell on-site energies from d (f) down
+    to s, SPE, Hubbard U and occupations in the same order), the mass/polynomial record (20 values),
+    nGrid - 1 rows of 2 x 10 (2 x 20) integrals, then the records after the line ``Spline``.
+    ``mass`` is the file's value (amu)."""
     if isinstance(path_or_text, str) and "\n" in path_or_text:
         lines = path_or_text.splitlines()
     else:
         with open(path_or_text) as fh:
             lines = fh.read().splitlines()
-    pos = 0
-    extended = lines[0].startswith("@")
-    if extended:
-        pos = 1
-    toks = lines[pos].replace(",", " ").split()
-    dist = float(toks[0])
-    n_rows = int(toks[1]) - 1
-    pos += 1
+    extended = bool(lines) and lines[0][:1] == "@"
+    rd = _ListDirected(lines, 1 if extended else 0)
+    head = rd.read(2)
+    dist = _num(head[0])
+    n_rows = int(_num(head[1])) - 1
     onsite = hubbu = occ = None
     mass = None
     n_shell = 4 if extended else 3
     if homo:
-        v = [float(x) for x in lines[pos].replace(",", " ").split()]
+        v = [_num(x) for x in rd.read(3 * n_shell + 1)]
         onsite = np.array(v[0:n_shell][::-1])
         hubbu = np.array(v[n_shell + 1:2 * n_shell + 1][::-1])
         occ = np.array(v[2 * n_shell + 1:3 * n_shell + 1][::-1])
-        pos += 1
-        mass = float(lines[pos].replace(",", " ").split()[0])
-        pos += 1
+        mass = _num(rd.read(20)[0])
     else:
-        pos += 1
+        rd.read(20)
     ham = np.zeros((n_rows, 20))
     over = np.zeros((n_rows, 20))
+    n_int = 20 if extended else 10
     for i in range(n_rows):
-        v = [float(x) for x in lines[pos + i].replace(",", " ").split()]
+        v = [_num(x) for x in rd.read(2 * n_int)]
         if extended:
             ham[i, :] = v[:20]
             over[i, :] = v[20:40]
@@ -148,25 +212,23 @@ def read_skf(path_or_text, homo: bool, read_repulsive: bool = True) -> SkfData:
             for k, slot in enumerate(OLD_SLOTS):
                 ham[i, slot - 1] = v[k]
                 over[i, slot - 1] = v[10 + k]
-    pos += n_rows
     rep = None
     if read_repulsive:
-        while pos < len(lines) and lines[pos].strip() != "Spline":
+        # the record must read "Spline" (trailing blanks allowed, as Fortran compares strings)
+        pos = 0
+        while pos < len(lines) and lines[pos].rstrip() != "Spline":
             pos += 1
         if pos >= len(lines):
             raise ValueError("No spline repulsive found in SKF data")
-        pos += 1
-        t = lines[pos].split()
-        n_spl, _ = int(t[0]), float(t[1])
-        pos += 1
-        exp_c = np.array([float(x) for x in lines[pos].split()[:3]])
-        pos += 1
+        rd = _ListDirected(lines, pos + 1)
+        t = rd.read(2)
+        n_spl = int(_num(t[0]))
+        exp_c = np.array([_num(x) for x in rd.read(3)])
         xs, xe, cub = [], [], []
         for _ in range(n_spl - 1):
-            v = [float(x) for x in lines[pos].split()]
+            v = [_num(x) for x in rd.read(6)]
             xs.append(v[0]); xe.append(v[1]); cub.append(v[2:6])
-            pos += 1
-        v = [float(x) for x in lines[pos].split()]
+        v = [_num(x) for x in rd.read(8)]
         xs.append(v[0]); xe.append(v[1])
         last = np.array(v[2:8])
         for j in range(1, n_spl):
