@@ -233,18 +233,12 @@ int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops
 int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *stream);
 
 /*
- * Stage-level test hooks (host arrays; used by the parity tests to check each eigensolver stage on
- * its own; they have no counterpart in the reference).
- *   dgemm:   c = alpha op(a) op(b) + beta c (column-major, lda=m or k as for op 'N'/'T').
- *   tridiag: Householder reduction of the symmetric a (n x n) -> d[n], e[n-1].
- *   stedc:   eigenpairs of the tridiagonal (d, e): d <- eigenvalues ascending, q[n*n] vectors.
- */
-/*
- * Tensor cores for the reduced-precision products (no reference counterpart): when enabled, FP32
- * GEMMs of the mixed form with m, n >= 256 run as split-BF16 compensated products on the tcgen05
- * tensor cores (FP32 accumulation, relative error ~2^-17) instead of FP32 FMA. Process-wide; returns
- * the previous setting. dftbgpu_test_gemm_tc runs one such product on host arrays (column-major,
- * flags as the library's triangular GEMM hints) for testing.
+ * Tensor cores for the perturbative updates of the mixed form (no reference counterpart): when
+ * enabled (the default), their FP32 products with m, n >= 128 run as split-BF16 compensated products
+ * on the tcgen05 tensor cores (three BF16 pieces per operand, six products, FP32 accumulation,
+ * relative error ~2^-22) instead of FP32 FMA. Process-wide; returns the previous setting.
+ * dftbgpu_test_gemm_tc runs one such product on host arrays (column-major, flags as the library's
+ * triangular GEMM hints) for testing.
  */
 int dftbgpu_set_tensor_cores(int enable);
 int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha, const float *a,
@@ -255,16 +249,23 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k
  * tridiagonalisation updates, divide-and-conquer merges, back-transformation, density and
  * energy-weighted density matrices) run as exact products of BF16 digit slices on the tcgen05
  * tensor cores: eight signed 7-bit digits per element at a power-of-two scale per row (column),
- * group sums exact in FP32 per 64-wide K block, int64 accumulation. The error is below 2^-52 of
- * max|A_ik| max|B_kj| K per element, like an FP64 product. The plain FP64 form always uses FP64
+ * group sums exact in FP32 per 64-wide K block, int64 accumulation. The error of an element is below
+ * K max|A_ik| max|B_kj| (2^-53 + K 2^-65), FP64-class. The plain FP64 form always uses FP64
  * arithmetic. Process-wide; returns the previous setting. dftbgpu_test_dgemm_tc runs one such
  * product on host arrays (column-major, flags as the library's triangular GEMM hints).
  */
 int dftbgpu_set_fp64_emulation(int enable);
 int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                           int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
-/* FP32 product of the mixed form's FP32 iterations (FP32 FMA; 128 x 128 tiles where they fill the GPU),
- * host arrays as dftbgpu_test_gemm_tc (no reference counterpart; a test hook). */
+/*
+ * Stage-level test hooks (host arrays; used by the parity tests to check each eigensolver stage on
+ * its own; they have no counterpart in the reference).
+ *   sgemm:   the FP32 FMA product of the mixed form's FP32 iterations (128 x 128 tiles where they
+ *            fill the GPU), arguments as dftbgpu_test_gemm_tc.
+ *   dgemm:   c = alpha op(a) op(b) + beta c (column-major, lda=m or k as for op 'N'/'T').
+ *   tridiag: Householder reduction of the symmetric a (n x n) -> d[n], e[n-1].
+ *   stedc:   eigenpairs of the tridiagonal (d, e): d <- eigenvalues ascending, q[n*n] vectors.
+ */
 int dftbgpu_test_sgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha, const float *a,
                        int lda, const float *b, int ldb, float beta, float *c, int ldc, int flags);
 int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
