@@ -398,6 +398,7 @@ class DftbGpu:
         self.species = np.asarray(species, dtype=np.int32)
         self.opts = default_opts(kT=kT, scc_tol=scc_tol, max_iter=max_iter, mix_alpha=mixing,
                                  precision=precision)
+        self._q_init = None      # atomic populations to start the SCC from (None: neutral atoms)
         self.set_geometry(coords)
 
     def set_geometry(self, coords, latvecs=None):
@@ -410,7 +411,29 @@ class DftbGpu:
 
     def _ensure(self):
         if self._res is None:
-            self._res = self.ctx.scc(self.opts)
+            self._res = self.ctx.scc(self.opts, q_init=self._q_init)
+
+    def _orbitals_per_atom(self):
+        return [self.model.species[s].n_orb for s in self.species]
+
+    def read_charges(self, path: str) -> None:
+        """Start the next SCC cycle from a reference charge restart file (``charges.dat`` /
+        ``charges.bin``, ``ReadInitialCharges = Yes``) instead of the neutral reference charges."""
+        from .restart import read_charges
+        n_orb = self._orbitals_per_atom()
+        q0 = sum(sum(self.model.species[s].occ) for s in self.species)
+        q = read_charges(path, n_orb, n_el=q0 - self.opts.net_charge)
+        offs = np.concatenate([[0], np.cumsum(n_orb)])
+        self._q_init = np.add.reduceat(q, offs[:-1]) if len(q) else q
+        self._res = None
+        self._grad = None
+
+    def write_charges(self, path: str) -> None:
+        """Write the converged orbital populations as a reference charge restart file (format 8;
+        ``.bin`` binary, otherwise ASCII), which DFTB+ reads with ``ReadInitialCharges = Yes``."""
+        from .restart import write_charges
+        self._ensure()
+        write_charges(path, self.ctx.orbital_populations(), self._orbitals_per_atom())
 
     def get_nr_atoms(self) -> int:
         return int(len(self.species))

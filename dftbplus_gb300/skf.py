@@ -21,6 +21,8 @@ from typing import Dict, List, Sequence, Tuple
 
 import numpy as np
 
+from .fortran_io import ListDirected
+
 # Slot (1-based, 20-slot spdf layout) of the integral (m, lMax, lMin); 0 = unused.
 # Same table as parser.F90:4088-4094 (reshaped column-major over (m, lMax, lMin)).
 _SLOT = {}
@@ -109,66 +111,6 @@ def write_skf(path_or_buf, dist: float, ham10: np.ndarray, over10: np.ndarray, *
             fh.write(text)
 
 
-class _ListDirected:
-    """Fortran list-directed input (``read(unit, *)``) over the records (lines) of a file, the way
-    the reference reads every SKF data line (``type/oldskdata.F90:139-202``, ``:233-262``).
-
-    Values are separated by blanks or a comma; ``r*c`` stands for r copies of c and ``r*`` for r null
-    values; two commas with nothing between are one null value; a slash ends the read (the items
-    left keep their values). A D exponent (``1.0D-3``) reads as E. One read consumes as many records
-    as it needs and drops the rest of its last record. Null values come back as None.
-    """
-
-    def __init__(self, lines: List[str], pos: int = 0):
-        self.lines = lines
-        self.pos = pos
-
-    @staticmethod
-    def _conv(tok: str) -> float:
-        return float(tok.replace("D", "E").replace("d", "e"))
-
-    @classmethod
-    def _items(cls, line: str):
-        """Values of one record in order, converted only when taken (None for a null, '/' for a
-        slash): a read stops taking items once it has enough, so the rest of the record may hold
-        anything."""
-        fields = line.split(",")
-        for fi, field in enumerate(fields):
-            toks = field.split()
-            if not toks:
-                # ",," or a leading comma: one null value (a trailing comma adds nothing)
-                if fi < len(fields) - 1:
-                    yield None
-                continue
-            for tok in toks:
-                if tok.startswith("/"):
-                    yield "/"
-                    return
-                if "*" in tok:
-                    r, c = tok.split("*", 1)
-                    val = None if c == "" else cls._conv(c)
-                    for _ in range(int(r)):
-                        yield val
-                else:
-                    yield cls._conv(tok)
-
-    def read(self, n: int) -> List[float | None]:
-        vals: List[float | None] = []
-        while len(vals) < n:
-            if self.pos >= len(self.lines):
-                raise ValueError("SKF data ended in the middle of a list-directed read")
-            line = self.lines[self.pos]
-            self.pos += 1
-            for item in self._items(line):
-                if isinstance(item, str):       # slash: the remaining items are not read
-                    vals.extend([None] * (n - len(vals)))
-                    break
-                vals.append(item)
-                if len(vals) == n:
-                    break
-        return vals
-
-
 def _num(v, default: float = 0.0) -> float:
     return default if v is None else float(v)
 
@@ -185,7 +127,7 @@ def read_skf(path_or_text, homo: bool, read_repulsive: bool = True) -> SkfData:
         with open(path_or_text) as fh:
             lines = fh.read().splitlines()
     extended = bool(lines) and lines[0][:1] == "@"
-    rd = _ListDirected(lines, 1 if extended else 0)
+    rd = ListDirected(lines, 1 if extended else 0)
     head = rd.read(2)
     dist = _num(head[0])
     n_rows = int(_num(head[1])) - 1
@@ -220,7 +162,7 @@ def read_skf(path_or_text, homo: bool, read_repulsive: bool = True) -> SkfData:
             pos += 1
         if pos >= len(lines):
             raise ValueError("No spline repulsive found in SKF data")
-        rd = _ListDirected(lines, pos + 1)
+        rd = ListDirected(lines, pos + 1)
         t = rd.read(2)
         n_spl = int(_num(t[0]))
         exp_c = np.array([_num(x) for x in rd.read(3)])

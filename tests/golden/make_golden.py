@@ -6,6 +6,8 @@
                         settings, 5 charge vectors and 4 difference vectors, tolerance 100 eps.
 * coulomb_cluster.json <- test/src/dftbp/unit/dftb/coulomb.F90:31-101 (``coulombderivcluster``):
                         2 atoms on the x axis 1 Bohr apart, charges +1/-1, expected dV/dR array.
+* charge_restart.json <- three charges.dat restart files of test/app/dftb+ (format 4, one spin
+                        channel, no block populations), their text and populations.
 """
 import json
 import os
@@ -53,6 +55,26 @@ def coulomb(ref):
             "expected_shape": [2, 3, 2], "expected_fortran_order": exp, "tol_eps_multiple": 1.0}
 
 
+CHARGE_FILES = ["test/app/dftb+/scc/H3_skipcheck/charges.dat",
+                "test/app/dftb+/scc/2H2O-3rdorder_read/charges.dat",
+                "test/app/dftb+/transport/deph_CH4-poisson/charges.dat"]
+
+
+def charges(ref):
+    """Spin-unpolarised, block-free ASCII charge restart files of the reference's application tests:
+    the text as it is, the orbital count of each atom (one record per atom in these files) and the
+    populations (records 3..) read with a plain split."""
+    out = []
+    for rel in CHARGE_FILES:
+        text = open(os.path.join(ref, rel)).read()
+        recs = [r for r in text.splitlines() if r.strip()]
+        rows = [[float(x) for x in r.split()] for r in recs[2:]]
+        out.append({"source": rel, "text": text, "n_orb_per_atom": [len(r) for r in rows],
+                    "populations": [x for r in rows for x in r],
+                    "checksum": float(recs[1].split()[-1])})
+    return out
+
+
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = os.path.dirname(os.path.abspath(__file__))
@@ -60,4 +82,6 @@ if __name__ == "__main__":
         json.dump(broyden(ref), fh, indent=1)
     with open(os.path.join(out, "coulomb_cluster.json"), "w") as fh:
         json.dump(coulomb(ref), fh, indent=1)
+    with open(os.path.join(out, "charge_restart.json"), "w") as fh:
+        json.dump(charges(ref), fh, indent=1)
     print("wrote", out)
