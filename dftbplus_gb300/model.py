@@ -8,6 +8,9 @@ integral tables on an equidistant grid and the spline repulsive.
 from __future__ import annotations
 
 import dataclasses
+import hashlib
+import json
+import os
 from typing import Dict, List, Sequence, Tuple
 
 import numpy as np
@@ -15,6 +18,16 @@ import numpy as np
 from .skf import SkfData, SplineRepulsive, full_table, n_integrals, read_skf
 
 MAX_SHELL = 4  # slots per species in the packed shell arrays (s, p, d, f)
+
+
+def _files_key(species: Sequence[Species], paths: Sequence[str]) -> str:
+    """SHA-256 over the requested shells and the bytes of every SKF file, in order."""
+    h = hashlib.sha256()
+    h.update(json.dumps([[x.name, list(x.shells)] for x in species]).encode())
+    for p in paths:
+        with open(p, "rb") as fh:
+            h.update(hashlib.sha256(fh.read()).digest())
+    return h.hexdigest()
 
 
 @dataclasses.dataclass
@@ -92,20 +105,69 @@ class Model:
         return cls(species, tables, reps)
 
     @classmethod
-    def from_files(cls, species: Sequence[Species], path_fmt: str) -> "Model":
-        """``path_fmt`` like ``"skf/{A}-{B}.skf"``; on-site/U/occ are taken from the homonuclear files."""
+    def from_files(cls, species: Sequence[Species], path_fmt: str, cache: str | None = None) -> "Model":
+        """``path_fmt`` like ``"skf/{A}-{B}.skf"``; on-site/U/occ are taken from the homonuclear files.
+
+        ``cache``: a binary table cache (``.npz``) keyed by the SHA-256 of the SKF files' bytes and the
+        requested shells: a matching cache is loaded without parsing, otherwise the files are parsed
+        and the cache is (re)written."""
         ns = len(species)
+        paths = [[path_fmt.format(A=species[a].name, B=species[b].name) for b in range(ns)] for a in range(ns)]
+        key = None
+        if cache is not None:
+            key = _files_key(species, [p for row in paths for p in row])
+            m = cls.load(cache, key)
+            if m is not None:
+                return m
         skf = {}
         for a in range(ns):
             for b in range(ns):
-                skf[(a, b)] = read_skf(path_fmt.format(A=species[a].name, B=species[b].name), homo=(a == b))
+                skf[(a, b)] = read_skf(paths[a][b], homo=(a == b))
         sp = []
         for a, s in enumerate(species):
             d = skf[(a, a)]
             sp.append(Species(s.name, list(s.shells), [float(d.onsite[l]) for l in s.shells],
                               float(d.hubbu[s.shells[0]]), [float(d.occ[l]) for l in s.shells],
                               float(d.mass)))
-        return cls.from_skf(sp, skf)
+        model = cls.from_skf(sp, skf)
+        if cache is not None:
+            model.save(cache, key)
+        return model
+
+    # ------------------------------------------------------------------ binary table cache
+    def save(self, path: str, key: str = "") -> None:
+        """All tables, repulsives and species data in one ``.npz`` (no pickled objects)."""
+        ns = self.n_species
+        arrs = {"key": np.array(key), "n_species": np.array(ns),
+                "species_json": np.array(json.dumps([dataclasses.asdict(x) for x in self.species]))}
+        for (a, b), t in self.tables.items():
+            arrs[f"dist_{a}_{b}"] = np.array(t.dist)
+            arrs[f"ham_{a}_{b}"] = t.ham
+            arrs[f"over_{a}_{b}"] = t.over
+            r = self.repulsives[(a, b)]
+            arrs[f"rep_{a}_{b}"] = r.pack()
+            arrs[f"repn_{a}_{b}"] = np.array(len(r.x_start))
+        tmp = path + ".tmp.npz"
+        np.savez(tmp, **arrs)
+        os.replace(tmp, path)
+
+    @classmethod
+    def load(cls, path: str, key: str | None = None) -> "Model | None":
+        """The model saved at ``path``; None if it is missing or its key differs from ``key``."""
+        if not os.path.exists(path):
+            return None
+        with np.load(path, allow_pickle=False) as z:
+            if key is not None and str(z["key"]) != key:
+                return None
+            ns = int(z["n_species"])
+            species = [Species(**d) for d in json.loads(str(z["species_json"]))]
+            tables, reps = {}, {}
+            for a in range(ns):
+                for b in range(ns):
+                    tables[(a, b)] = PairTable(dist=float(z[f"dist_{a}_{b}"]), ham=np.array(z[f"ham_{a}_{b}"]),
+                                               over=np.array(z[f"over_{a}_{b}"]))
+                    reps[(a, b)] = SplineRepulsive.unpack(np.array(z[f"rep_{a}_{b}"]), int(z[f"repn_{a}_{b}"]))
+        return cls(species, tables, reps)
 
     # ------------------------------------------------------------------ packing for the C-ABI
     def pack(self) -> dict:

@@ -57,6 +57,16 @@ class SplineRepulsive:
         return np.concatenate([[self.cutoff], self.exp_coeffs, self.x_start,
                                self.sp_coeffs.reshape(-1), self.last_coeffs]).astype(np.float64)
 
+    @classmethod
+    def unpack(cls, flat: np.ndarray, n_spline: int) -> "SplineRepulsive":
+        """Inverse of ``pack`` for a spline of ``n_spline`` segments."""
+        f = np.asarray(flat, dtype=np.float64)
+        x0 = 4
+        c0 = x0 + n_spline
+        l0 = c0 + 4 * (n_spline - 1)
+        return cls(cutoff=float(f[0]), exp_coeffs=f[1:4].copy(), x_start=f[x0:c0].copy(),
+                   sp_coeffs=f[c0:l0].reshape(n_spline - 1, 4).copy(), last_coeffs=f[l0:l0 + 6].copy())
+
 
 @dataclasses.dataclass
 class SkfData:

@@ -88,3 +88,34 @@ def test_truncated_file_reports():
     lines = text.splitlines()[:5]
     with pytest.raises(ValueError):
         skf.read_skf("\n".join(lines), homo=True, read_repulsive=False)
+
+
+def test_binary_table_cache(tmp_path, monkeypatch, water_model):
+    """Model.from_files(cache=...) parses once and writes an .npz keyed by the SKF bytes; a matching
+    cache is loaded without parsing and packs to the same C-ABI arrays; a changed file is reparsed."""
+    from dftbplus_gb300 import synth
+    from dftbplus_gb300 import model as model_mod
+    sset = synth.make_skf_set([synth.SPECIES_O, synth.SPECIES_H], synth.WATER_SEED, synth.WATER_DRAW)
+    names = ["O", "H"]
+    for (a, b), d in sset.items():
+        h10, s10 = synth.skf_columns10(d)
+        homo = (d.onsite, d.hubbu, d.occ, d.mass) if a == b else None
+        skf.write_skf(str(tmp_path / f"{names[a]}-{names[b]}.skf"), d.dist, h10, s10, homo=homo,
+                      repulsive=d.repulsive)
+    fmt = str(tmp_path / "{A}-{B}.skf")
+    cache = str(tmp_path / "tables.npz")
+    sp = [synth.SPECIES_O, synth.SPECIES_H]
+    m1 = model_mod.Model.from_files(sp, fmt, cache=cache)
+    parsed = []
+    real_read = model_mod.read_skf
+    monkeypatch.setattr(model_mod, "read_skf", lambda *a, **k: parsed.append(a) or real_read(*a, **k))
+    m2 = model_mod.Model.from_files(sp, fmt, cache=cache)
+    assert not parsed                                   # served from the cache
+    p1, p2 = m1.pack(), m2.pack()
+    for k in p1:
+        assert np.array_equal(np.asarray(p1[k]), np.asarray(p2[k])), k
+    assert [x.mass for x in m2.species] == [x.mass for x in m1.species]
+    with open(str(tmp_path / "O-H.skf"), "a") as fh:     # any change of the bytes invalidates it
+        fh.write("\n")
+    model_mod.Model.from_files(sp, fmt, cache=cache)
+    assert parsed
