@@ -75,7 +75,11 @@ _COL10 = {(2, 2, 0): 0, (2, 2, 1): 1, (2, 2, 2): 2, (1, 2, 0): 3, (1, 2, 1): 4,
 
 def _repulsive(K: float, beta: float, rc: float = REP_CUTOFF, r0: float = 1.0,
                seg: float = 0.1) -> SplineRepulsive:
-    """Piecewise-polynomial form of g(r) = K e^{-beta r} - T2(r), T2 = Taylor(2) of K e^{-beta r} at rc."""
+    """Spline form of g(r) = K e^{-beta r} - T2(r), T2 = Taylor(2) of K e^{-beta r} at rc, as an SKF
+    ``Spline`` block: cubic Hermite segments through g and g' at the knots (value and slope continuous
+    at every knot, so MD conserves energy), a quintic last segment matching g, g', g'' at its start and
+    reaching zero value, slope and curvature at the cutoff, and the exponential head
+    e^{-a1 r + a2} + a3 matching g and g' at the first knot."""
     e_rc = K * math.exp(-beta * rc)
 
     def deriv(r, k):  # k-th derivative of g
@@ -91,9 +95,23 @@ def _repulsive(K: float, beta: float, rc: float = REP_CUTOFF, r0: float = 1.0,
 
     n_spl = int(round((rc - r0) / seg))
     xs = r0 + seg * np.arange(n_spl)
-    cub = np.array([[deriv(x, 0), deriv(x, 1), deriv(x, 2) / 2.0, deriv(x, 3) / 6.0] for x in xs[:-1]])
+    cub = []
+    for j in range(n_spl - 1):
+        h = xs[j + 1] - xs[j]
+        y0, y1 = deriv(xs[j], 0), deriv(xs[j + 1], 0)
+        d0, d1 = deriv(xs[j], 1), deriv(xs[j + 1], 1)
+        c2 = (3.0 * (y1 - y0) / h - 2.0 * d0 - d1) / h
+        c3 = (d0 + d1 - 2.0 * (y1 - y0) / h) / (h * h)
+        cub.append([y0, d0, c2, c3])
+    cub = np.array(cub)
     xl = xs[-1]
-    last = np.array([deriv(xl, k) / math.factorial(k) for k in range(6)])
+    # quintic on [xl, rc]: (g, g', g'') at xl, zero value, slope and curvature at rc
+    h = rc - xl
+    y, d, c = deriv(xl, 0), deriv(xl, 1), deriv(xl, 2) / 2.0
+    m = np.array([[h ** 3, h ** 4, h ** 5], [3 * h ** 2, 4 * h ** 3, 5 * h ** 4], [6 * h, 12 * h ** 2, 20 * h ** 3]])
+    rhs = -np.array([y + d * h + c * h * h, d + 2 * c * h, 2 * c])
+    c345 = np.linalg.solve(m, rhs)
+    last = np.array([y, d, c, c345[0], c345[1], c345[2]])
     g0, g1 = deriv(r0, 0), deriv(r0, 1)
     a1 = -g1 / g0
     a2 = math.log(g0) + a1 * r0
