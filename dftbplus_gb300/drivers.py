@@ -1,5 +1,6 @@
-"""Geometry drivers with resident state: velocity Verlet molecular dynamics and FIRE relaxation over
-a calculator (``binding.DftbGpu`` on the GPU).
+"""Geometry drivers with resident state: velocity Verlet molecular dynamics (also with
+extended-Lagrangian charge propagation, XLBOMD) and FIRE relaxation over a calculator
+(``binding.DftbGpu`` on the GPU).
 
 Between geometry steps the SCC cycle starts from the previous step's converged charges, as the
 reference carries ``qInput`` over from one geometry to the next, and the device keeps its model,
@@ -82,6 +83,120 @@ def run_md(calc, coords: np.ndarray, masses_amu: np.ndarray, dt: float, n_steps:
         if callback is not None:
             callback(step, x, v, epot, ekin)
         x = x_new
+    return x, v, energies
+
+
+# Dissipation coefficients of the extended-Lagrangian integrator for K = 5, 6, 7 auxiliary
+# generations (md/extlagrangian.F90:80-96; Niklasson et al., J. Chem. Phys. 130, 214109 (2009)),
+# kept identical because they define the integrator: (coefficients c_0..c_K, alpha, kappa).
+_XL_COEFFS = {
+    5: ([-6.0, 14.0, -8.0, -3.0, 4.0, -1.0], 18e-3, 1.82),
+    6: ([-14.0, 36.0, -27.0, -2.0, 12.0, -6.0, 1.0], 5.5e-3, 1.84),
+    7: ([-36.0, 99.0, -88.0, 11.0, 32.0, -25.0, 8.0, -1.0], 1.6e-3, 1.86),
+}
+
+
+class ExtLagrangian:
+    """Extended-Lagrangian propagation of the SCC input charges (md/extlagrangian.F90): off (the next
+    input is the last output), filling the history with K + 1 converged outputs, then for each step
+    n(t + dt) = 2 n(t) - n(t - dt) + kappa s (q(t) - n(t)) + alpha sum_i c_i n(t - i dt), where q(t)
+    is the SCC output at t and the n are the auxiliary charges kept in a ring of K + 1."""
+
+    OFF, FILLING, INTERPOLATING, ON = 1, 2, 3, 4
+
+    def __init__(self, n_elems: int, n_kappa: int = 5, scale: float = 1.0):
+        if n_kappa not in _XL_COEFFS:
+            raise ValueError("the number of integration steps must be 5, 6 or 7")
+        coeffs, self.alpha, self.kappa = _XL_COEFFS[n_kappa]
+        self.coeffs = np.array(coeffs)
+        self.k = n_kappa
+        self.scale = scale
+        self.aux = np.zeros((n_elems, n_kappa + 1))
+        self.ind = 0                  # 1-based slot of the newest vector (0 before the first)
+        self.phase = self.OFF
+        self.i_step, self.n_steps, self.n_transient = 1, 0, 0
+
+    def _mod(self, ind: int) -> int:
+        return (ind - 1) % (self.k + 1) + 1
+
+    def turn_on(self, n_transient: int = 0) -> None:
+        self.phase = self.FILLING
+        self.i_step = 1
+        self.n_steps = self.k + 1
+        self.n_transient = n_transient
+
+    def needs_converged(self) -> bool:
+        return self.phase in (self.OFF, self.FILLING, self.INTERPOLATING)
+
+    def next_input(self, q_out: np.ndarray) -> np.ndarray:
+        q_out = np.asarray(q_out, dtype=np.float64)
+        if self.phase == self.OFF:
+            nxt = q_out.copy()
+        elif self.phase == self.FILLING:
+            self.ind = self._mod(self.ind + 1)
+            self.aux[:, self.ind - 1] = q_out
+            nxt = q_out.copy()
+        else:
+            i0 = self.ind
+            if self.phase == self.INTERPOLATING:
+                cc = self.i_step / (self.n_steps + 1)
+                self.aux[:, i0 - 1] = cc * self.aux[:, i0 - 1] + (1.0 - cc) * q_out
+            i1 = self._mod(i0 - 1)
+            nxt = 2.0 * self.aux[:, i0 - 1] - self.aux[:, i1 - 1]
+            nxt = nxt + self.kappa * self.scale * (q_out - self.aux[:, i0 - 1])
+            for i in range(self.k + 1):
+                nxt = nxt + self.alpha * self.coeffs[i] * self.aux[:, self._mod(i0 - i) - 1]
+            self.ind = self._mod(self.ind + 1)
+            self.aux[:, self.ind - 1] = nxt
+        self._advance()
+        return nxt
+
+    def _advance(self) -> None:
+        if self.phase in (self.OFF, self.ON):
+            return
+        self.i_step += 1
+        if self.phase == self.FILLING and self.i_step > self.n_steps:
+            self.phase, self.i_step, self.n_steps = self.INTERPOLATING, 1, self.n_transient
+        if self.phase == self.INTERPOLATING and self.i_step > self.n_steps:
+            self.phase = self.ON
+
+
+def run_xlbomd(calc, coords: np.ndarray, masses_amu: np.ndarray, dt: float, n_steps: int,
+               velocities: Optional[np.ndarray] = None, n_kappa: int = 5, pre_steps: int = 0,
+               min_scc_iter: int = 1, max_scc_iter: int = 200, scc_tol: float = 1e-5):
+    """Velocity Verlet MD whose SCC input charges are propagated by the extended Lagrangian
+    (md/xlbomd.F90, the ``Xlbomd`` block): fully converged SCC cycles until K + 1 outputs fill the
+    history (started after ``pre_steps``), then each step starts from the propagated charges and
+    stops at ``scc_tol`` within ``min_scc_iter``..``max_scc_iter`` iterations. ``calc.opts`` carries
+    the calculator's own SCC settings for the converged steps. Returns what ``run_md`` returns."""
+    m = np.asarray(masses_amu, dtype=np.float64) * AMU_AU
+    x = np.array(coords, dtype=np.float64)
+    vv = VelocityVerlet(dt, x, velocities)
+    xl = None
+    start_xl = pre_steps + 1          # nPreSteps + nFullSccSteps - nKappa, nFullSccSteps = K + 1
+    full = (calc.opts.min_iter, calc.opts.max_iter, calc.opts.scc_tol)
+    energies: List[tuple] = []
+    v = vv.velocities.copy()
+    try:
+        for step in range(n_steps + 1):
+            if xl is not None and not xl.needs_converged():
+                calc.opts.min_iter, calc.opts.max_iter, calc.opts.scc_tol = min_scc_iter, max_scc_iter, scc_tol
+            else:
+                calc.opts.min_iter, calc.opts.max_iter, calc.opts.scc_tol = full
+            calc.set_geometry(x)
+            epot = calc.get_energy()
+            grad = np.asarray(calc.get_gradients(), dtype=np.float64).T
+            q_out = np.array(calc._res["q_out"], dtype=np.float64)
+            if xl is None:
+                xl = ExtLagrangian(len(q_out), n_kappa)
+            if step + 1 == start_xl:
+                xl.turn_on(0)
+            calc._q_init = xl.next_input(q_out)
+            x_new, v = vv.next(-grad / m[None, :])
+            energies.append((epot, 0.5 * float(np.sum(m[None, :] * v * v))))
+            x = x_new
+    finally:
+        calc.opts.min_iter, calc.opts.max_iter, calc.opts.scc_tol = full
     return x, v, energies
 
 

@@ -29,8 +29,11 @@ class _OracleCalc:
     """The CPU oracle behind the calculator protocol of binding.DftbGpu (test infrastructure)."""
 
     def __init__(self, model, coords, species):
+        from dftbplus_gb300 import binding
         self.model, self.species = model, np.asarray(species)
         self._q_init, self.iters = None, []
+        self.opts = binding.SccOpts()           # the calculator's SCC settings, as DftbGpu.opts
+        self.opts.min_iter, self.opts.max_iter, self.opts.scc_tol = 1, 100, 1e-9
         self.set_geometry(coords)
 
     def set_geometry(self, x):
@@ -39,7 +42,8 @@ class _OracleCalc:
 
     def _ensure(self):
         if self._res is None:
-            r = O.run_scc(self.sys, kt=1e-3, scc_tol=1e-9, q_init_atom=self._q_init)
+            r = O.run_scc(self.sys, kt=1e-3, scc_tol=self.opts.scc_tol, max_iter=self.opts.max_iter,
+                          q_init_atom=self._q_init)
             self.iters.append(r.n_iter)
             self._ref = r
             self._res = {"q_out": r.q_out_atom, "energies": r.energies}
@@ -131,3 +135,43 @@ def test_fire_reference_steps():
     assert f.dt > 0.1 and f.a < 0.1
     f.step(np.array([-1.0]))                             # the velocity now points uphill
     assert f.a == 0.1 and f.reset_step == f.iter - 1
+
+
+def test_ext_lagrangian_phases_and_fixed_point():
+    """md/extlagrangian.F90: after turnOn the integrator wants K + 1 converged outputs, then predicts;
+    a constant output is a fixed point (the dissipation coefficients sum to zero)."""
+    for k in (5, 6, 7):
+        xl = drivers.ExtLagrangian(3, n_kappa=k)
+        assert abs(sum(xl.coeffs)) < 1e-12
+        q = np.array([6.1, 0.95, 0.95])
+        assert np.array_equal(xl.next_input(q), q) and xl.needs_converged()      # off
+        xl.turn_on(0)
+        for _ in range(k + 1):
+            assert xl.needs_converged()
+            assert np.array_equal(xl.next_input(q), q)
+        assert not xl.needs_converged()
+        for _ in range(5):
+            assert np.allclose(xl.next_input(q), q, atol=1e-13)
+    with pytest.raises(ValueError):
+        drivers.ExtLagrangian(3, n_kappa=4)
+
+
+def test_xlbomd_oracle(water_model):
+    """XLBOMD on relaxed (H2O)2 with the oracle: SCC cycles started from the propagated charges and
+    stopped at 1e-5 e take far fewer iterations than converged cycles started from the previous
+    charges, with the same energy conservation and a trajectory within 1e-5 Bohr."""
+    from dftbplus_gb300 import synth
+    c, s = synth.water_cluster(2, 4.0, 3)
+    calc = _OracleCalc(water_model, c, s)
+    x, _, _, _ = drivers.relax(calc, c, tol=1e-5, max_steps=2000, dt_max=20.0)
+    masses = np.array([water_model.species[q].mass for q in s])
+    v0 = np.random.default_rng(0).normal(0.0, 2e-4, c.shape)
+    ref = _OracleCalc(water_model, x, s)
+    x_ref, _, en_ref = drivers.run_md(ref, x, masses, 10.0, 30, velocities=v0)
+    xl = _OracleCalc(water_model, x, s)
+    x_xl, _, en_xl = drivers.run_xlbomd(xl, x, masses, 10.0, 30, velocities=v0, scc_tol=1e-5)
+    assert sum(xl.iters) < 0.7 * sum(ref.iters)
+    spread = lambda en: np.ptp([a + b for a, b in en])
+    assert spread(en_xl) < 1.2 * spread(en_ref) + 1e-9
+    assert np.max(np.abs(x_xl - x_ref)) < 1e-5
+    assert xl.opts.scc_tol == 1e-9 and xl.opts.max_iter == 100        # settings restored
