@@ -48,12 +48,21 @@ def _workload(name):
 BATCH_NMOL, BATCH_SEED = 4096, 4096
 
 
+def batch_sizes(nmol=BATCH_NMOL, seed=BATCH_SEED):
+    """Waters per molecule of the batched set: n seeded uniform in [2, 48]."""
+    return np.random.default_rng(seed).integers(2, 49, nmol)
+
+
+def batch_molecule(i, n):
+    """Molecule i of the batched set: (H2O)n in a sphere of radius 10 (n/32)^(1/3) A, seed 10000 + i."""
+    from dftbplus_gb300 import synth
+    return synth.water_cluster(int(n), 10.0 * (n / 32.0) ** (1.0 / 3.0), 10000 + i)
+
+
 def _batch_workload(nmol=BATCH_NMOL, seed=BATCH_SEED):
     """4,096 independent (H2O)n clusters, n seeded uniform in [2, 48], sphere radius 10 (n/32)^(1/3) A."""
     from dftbplus_gb300 import synth
-    rng = np.random.default_rng(seed)
-    ns = rng.integers(2, 49, nmol)
-    mols = [synth.water_cluster(int(n), 10.0 * (n / 32.0) ** (1.0 / 3.0), 10000 + i) for i, n in enumerate(ns)]
+    mols = [batch_molecule(i, n) for i, n in enumerate(batch_sizes(nmol, seed))]
     return synth.water_model(), mols
 
 

@@ -389,6 +389,10 @@ class DftbGpu:
     """SCC-DFTB calculator on one GB300, API-compatible with the reference's ``DftbPlus`` for
     the non-periodic energy/gradient/charge queries."""
 
+    # dftbgpu_scc accepts at most this many SCC iterations (the Broyden history of the device mixer
+    # lives in one CTA's shared memory); geometry drivers clamp their iteration limits to it
+    MAX_SCC_ITER = 150
+
     def __init__(self, model: Model, coords: np.ndarray, species: np.ndarray, kT: float = 1e-3,
                  scc_tol: float = 1e-7, max_iter: int = 100, mixing: float = 0.2, device: int = 0,
                  precision: int = PREC_FP64):

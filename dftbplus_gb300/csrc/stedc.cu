@@ -755,7 +755,13 @@ extern "C" int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *
     g_noalloc_dev_ptr[dev] = ptr;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the merge products go through dgemm; with the calling thread's tensor-core routing flag set it
+  // would send them to tc_dgemm, whose per-thread scratch is allocated on first use. Keep the FP64
+  // FMA kernel (no workspace) for this call.
+  const bool tc_route = dg::g_tc_dgemm;
+  dg::g_tc_dgemm = false;
   int st = dg::stedc_noalloc_impl(s, n, d, e, q, g_noalloc_dev_ptr[dev]);
+  dg::g_tc_dgemm = tc_route;
   if (cudaGetLastError() != cudaSuccess) return DFTBGPU_ERR_CUDA;
   if (st == dg::kDevIterCap) return DFTBGPU_ERR_ITER_CAP;
   return st == 0 ? DFTBGPU_OK : DFTBGPU_ERR_CUDA;

@@ -88,11 +88,13 @@ def run_md(calc, coords: np.ndarray, masses_amu: np.ndarray, dt: float, n_steps:
 
 # Dissipation coefficients of the extended-Lagrangian integrator for K = 5, 6, 7 auxiliary
 # generations (md/extlagrangian.F90:80-96; Niklasson et al., J. Chem. Phys. 130, 214109 (2009)),
-# kept identical because they define the integrator: (coefficients c_0..c_K, alpha, kappa).
+# kept identical because they define the integrator: (coefficients c_0..c_K, alpha, kappa). The
+# reference declares the K = 7 alpha without a kind suffix, so Fortran stores the single-precision
+# value of 1.6e-3; np.float32 reproduces that value bit for bit.
 _XL_COEFFS = {
     5: ([-6.0, 14.0, -8.0, -3.0, 4.0, -1.0], 18e-3, 1.82),
     6: ([-14.0, 36.0, -27.0, -2.0, 12.0, -6.0, 1.0], 5.5e-3, 1.84),
-    7: ([-36.0, 99.0, -88.0, 11.0, 32.0, -25.0, 8.0, -1.0], 1.6e-3, 1.86),
+    7: ([-36.0, 99.0, -88.0, 11.0, 32.0, -25.0, 8.0, -1.0], float(np.float32(1.6e-3)), 1.86),
 }
 
 
@@ -168,7 +170,12 @@ def run_xlbomd(calc, coords: np.ndarray, masses_amu: np.ndarray, dt: float, n_st
     (md/xlbomd.F90, the ``Xlbomd`` block): fully converged SCC cycles until K + 1 outputs fill the
     history (started after ``pre_steps``), then each step starts from the propagated charges and
     stops at ``scc_tol`` within ``min_scc_iter``..``max_scc_iter`` iterations. ``calc.opts`` carries
-    the calculator's own SCC settings for the converged steps. Returns what ``run_md`` returns."""
+    the calculator's own SCC settings for the converged steps. A calculator that bounds its SCC
+    iterations (``calc.MAX_SCC_ITER``, the GPU engine's 150) gets ``max_scc_iter`` clamped to that
+    bound. Returns what ``run_md`` returns."""
+    max_scc_iter = min(int(max_scc_iter), int(getattr(calc, "MAX_SCC_ITER", max_scc_iter)))
+    if max_scc_iter < min_scc_iter:
+        raise ValueError(f"max_scc_iter {max_scc_iter} < min_scc_iter {min_scc_iter}")
     m = np.asarray(masses_amu, dtype=np.float64) * AMU_AU
     x = np.array(coords, dtype=np.float64)
     vv = VelocityVerlet(dt, x, velocities)

@@ -19,10 +19,16 @@ from .skf import SkfData, SplineRepulsive, full_table, n_integrals, read_skf
 
 MAX_SHELL = 4  # slots per species in the packed shell arrays (s, p, d, f)
 
+# Layout version of the binary table cache (the .npz written by Model.save). It enters the cache
+# key and is stored in the file; a cache of another version is treated as a miss and rewritten, so
+# a change to full_table, SplineRepulsive.pack/unpack or the .npz layout must bump it.
+CACHE_FORMAT = 2
+
 
 def _files_key(species: Sequence[Species], paths: Sequence[str]) -> str:
-    """SHA-256 over the requested shells and the bytes of every SKF file, in order."""
+    """SHA-256 over the cache format, the requested shells and the bytes of every SKF file, in order."""
     h = hashlib.sha256()
+    h.update(f"dftbgpu-table-cache-v{CACHE_FORMAT}".encode())
     h.update(json.dumps([[x.name, list(x.shells)] for x in species]).encode())
     for p in paths:
         with open(p, "rb") as fh:
@@ -138,7 +144,7 @@ class Model:
     def save(self, path: str, key: str = "") -> None:
         """All tables, repulsives and species data in one ``.npz`` (no pickled objects)."""
         ns = self.n_species
-        arrs = {"key": np.array(key), "n_species": np.array(ns),
+        arrs = {"key": np.array(key), "format": np.array(CACHE_FORMAT), "n_species": np.array(ns),
                 "species_json": np.array(json.dumps([dataclasses.asdict(x) for x in self.species]))}
         for (a, b), t in self.tables.items():
             arrs[f"dist_{a}_{b}"] = np.array(t.dist)
@@ -153,10 +159,13 @@ class Model:
 
     @classmethod
     def load(cls, path: str, key: str | None = None) -> "Model | None":
-        """The model saved at ``path``; None if it is missing or its key differs from ``key``."""
+        """The model saved at ``path``; None if it is missing, was written in another cache format,
+        or its key differs from ``key``."""
         if not os.path.exists(path):
             return None
         with np.load(path, allow_pickle=False) as z:
+            if "format" not in z.files or int(z["format"]) != CACHE_FORMAT:
+                return None
             if key is not None and str(z["key"]) != key:
                 return None
             ns = int(z["n_species"])

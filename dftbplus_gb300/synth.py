@@ -36,8 +36,11 @@ SPECIES_O = Species("O", [0, 1], [-0.87, -0.33], 0.50, [2.0, 4.0], 16.0)
 SPECIES_H = Species("H", [0], [-0.24], 0.42, [1.0], 1.008)
 SPECIES_TI = Species("Ti", [0, 1, 2], [-0.17, -0.06, -0.20], 0.32, [2.0, 0.0, 2.0], 47.87)
 
-# Draw index accepted by the table search in oracle/select_tables.py (lambda_min(S) >= 0.2 on the
-# water workloads and a HOMO-LUMO gap well above kT); tests re-verify it.
+# The water tables use draw k = WATER_DRAW of rng = default_rng([WATER_SEED, k]): draws were tried in
+# order k = 0, 1, 2, ... and the first accepted whose overlap has lambda_min(S) >= 0.2 on the (H2O)32
+# (10 A, seed 1) and (H2O)128 (20 A, seed 128) clusters and whose (H2O)32 SCC HOMO-LUMO gap exceeds
+# 0.1 Ha (100 kT). Draws 0, 2 and 3 give an indefinite overlap, draw 1 a gap of 0.096 Ha;
+# tests/test_workloads.py re-verifies both criteria for the accepted draw.
 WATER_SEED = 20261204
 WATER_DRAW = 4
 

@@ -217,18 +217,20 @@ int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops
 
 /*
  * Allocation-free tridiagonal divide and conquer. This entry point has no counterpart in the
- * reference. It serves callers that cannot allocate device memory: a solver step recorded into a
- * CUDA graph (cudaMalloc is not permitted during stream capture), a host program whose device
- * memory belongs to another allocator or pool, or a dynamics loop that must avoid the device-wide
- * synchronisation an allocation implies. It needs no context.
+ * reference. It serves callers that cannot call cudaMalloc: a host program whose device memory is
+ * all held by another allocator or memory pool (an extra cudaMalloc would fail or fragment it), and
+ * a time-stepping loop that must not let an allocation synchronise the whole device between steps.
+ * It needs no context and allocates nothing.
  *   n in 1..256 (larger n returns DFTBGPU_ERR_ARGS and does nothing);
  *   d[n] (device): diagonal in, eigenvalues ascending out; e[n-1] (device): off-diagonal, read only;
  *   q[n*n] (device, column-major): eigenvectors out; stream: cudaStream_t or NULL (legacy default).
  * The caller passes inputs and outputs; all scratch is one file-scope device array of about 2.2 MB
  * that every GPU loading the library keeps until process exit. The first call on a device looks
- * up that array's device address (make it before any stream capture). Calls share the array, so
- * calls that overlap on the GPU (other streams or threads) race and must be serialised by the
- * caller. Returns 0, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_ITER_CAP or DFTBGPU_ERR_CUDA.
+ * up that array's device address with cudaGetSymbolAddress; make that first call before any stream
+ * capture. Calls share the array and it keeps the last call's contents (each call clears what must
+ * start at zero), so calls that overlap on the GPU (other streams or threads) race and must be
+ * serialised by the caller. The call waits for its stream before returning (it reads its status
+ * word back). Returns 0, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_ITER_CAP or DFTBGPU_ERR_CUDA.
  */
 int dftbgpu_stedc_noalloc(int n, double *d, const double *e, double *q, void *stream);
 

@@ -151,3 +151,42 @@ def test_batch_mixed_spd_fractional(gpu_lib, tio2_model):
         assert abs(res["energies"][i]["EMermin"] - ref.energies["EMermin"]) / len(s) < 1e-8
         assert np.max(np.abs(grads[i] - O.gradients(sys_, ref))) < 1e-6
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_largest_molecules_of_benchmark_set(gpu_lib, water_model, precision):
+    """The largest molecules of the 4,096-molecule benchmark set (40-48 waters, 240-288 orbitals, the
+    regime of long QL sweeps, large merges and slabs beyond shared memory), batched together with a
+    few small ones: every molecule against the oracle run on it alone (FP64 at the single-system FP64
+    tolerances, mixed at 1e-8 Ha/atom and 1e-6 Ha/Bohr)."""
+    from dftbplus_gb300 import binding
+    from bench import batch_sizes, batch_molecule
+    ns = batch_sizes()
+    big = [i for i, n in enumerate(ns) if n >= 40]
+    pick = sorted(set([i for i in big if ns[i] == 48][:2] + big[:6] + [int(np.argmin(ns)), 7]))
+    mols = [batch_molecule(i, ns[i]) for i in pick]
+    assert max(len(m[1]) for m in mols) == 144 and min(len(m[1]) for m in mols) == 6
+    ctx = _ctx(water_model)
+    ctx.batch_set_geometries([m[0] for m in mols], [m[1] for m in mols])
+    prec = binding.PREC_MIXED if precision == "mixed" else binding.PREC_FP64
+    res = ctx.batch_scc(binding.default_opts(kT=1e-3, scc_tol=1e-7, precision=prec))
+    grads = ctx.batch_gradients()
+    off = ctx.batch_atom_off
+    for i, (c, s) in enumerate(mols):
+        sys_ = O.System(water_model, c, s)
+        ref = O.run_scc(sys_, kt=1e-3, scc_tol=1e-7)
+        assert res["converged"][i] and ref.converged
+        gref = O.gradients(sys_, ref)
+        e = res["energies"][i]
+        q = res["q_out"][off[i]:off[i + 1]]
+        if precision == "fp64":
+            assert res["n_iter"][i] == ref.n_iter, (pick[i], res["n_iter"][i], ref.n_iter)
+            for k in ("EnonSCC", "Escc", "Erep", "Etotal", "EMermin", "TS", "Eband"):
+                assert abs(e[k] - ref.energies[k]) < 1e-9, (pick[i], k, e[k], ref.energies[k])
+            assert np.max(np.abs(q - ref.q_out_atom)) < 1e-8
+            assert np.max(np.abs(grads[i] - gref)) < 1e-8, (pick[i], np.max(np.abs(grads[i] - gref)))
+        else:
+            assert abs(e["EMermin"] - ref.energies["EMermin"]) / len(s) < 1e-8
+            assert np.max(np.abs(q - ref.q_out_atom)) < 1e-6
+            assert np.max(np.abs(grads[i] - gref)) < 1e-6
+    ctx.close()

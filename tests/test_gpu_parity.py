@@ -196,8 +196,17 @@ def test_mixed_fp64_products_on_tensor_cores(gpu_lib, water_model):
         for emulate in (True, False):
             binding.set_fp64_emulation(emulate)
             ctx = _ctx(water_model, c, s)
+            ctx.profile(True)
             res = ctx.scc(binding.default_opts(kT=1e-3, scc_tol=1e-7, precision=binding.PREC_MIXED))
+            prof = ctx.profile_read()
+            ctx.profile(False)
             assert res["converged"]
+            # the route is what the test is about: on, some FP64 products ran on the tensor cores;
+            # off, none did
+            if emulate:
+                assert prof["gemm_tc_fp64"]["calls"] > 0, "no FP64 product ran on the tensor cores"
+            else:
+                assert prof["gemm_tc_fp64"]["calls"] == 0
             out[emulate] = (res["energies"]["EMermin"], res["q_out"], ctx.gradients())
             ctx.close()
     finally:

@@ -109,3 +109,29 @@ def test_scc_charge_conservation(water_model):
     res = O.run_scc(sys_)
     assert res.converged
     assert abs(res.q_out_atom.sum() - sys_.q0_atom.sum()) < 1e-9
+
+
+def test_scc_golden_fixtures_reproduce():
+    """The committed end-to-end fixtures of the benchmark workloads belong to the current workload
+    generator (geometry digest), and the (H2O)128 one is reproduced by the oracle to rounding."""
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    from make_scc_golden import geometry_digest, ENERGY_KEYS
+    from bench import CONFIGS
+    from dftbplus_gb300 import synth
+    for name in ("h2o128", "h2o1024"):
+        z = np.load(os.path.join(here, f"scc_{name}.npz"))
+        n_mol, radius, seed = CONFIGS[name]
+        c, s = synth.water_cluster(n_mol, radius, seed)
+        assert str(z["geometry_sha256"]) == geometry_digest(c, s)
+        assert bool(z["converged"]) and z["errors"][-1] < 1e-7
+        assert z["grad"].shape == (3, len(s)) and z["q_out_atom"].shape == (len(s),)
+    z = np.load(os.path.join(here, "scc_h2o128.npz"))
+    c, s = synth.water_cluster(*CONFIGS["h2o128"])
+    sys_ = O.System(synth.water_model(), c, s)
+    res = O.run_scc(sys_, kt=1e-3, scc_tol=1e-7)
+    assert res.n_iter == int(z["n_iter"])
+    assert np.allclose([res.energies[k] for k in ENERGY_KEYS], z["energies"], atol=1e-10, rtol=0)
+    assert np.allclose(res.q_out_atom, z["q_out_atom"], atol=1e-10, rtol=0)

@@ -119,3 +119,28 @@ def test_binary_table_cache(tmp_path, monkeypatch, water_model):
         fh.write("\n")
     model_mod.Model.from_files(sp, fmt, cache=cache)
     assert parsed
+
+
+def test_table_cache_format_mismatch_is_a_miss(tmp_path, monkeypatch):
+    """A cache written in another layout version is not loaded (treated as a miss and rewritten)."""
+    from dftbplus_gb300 import synth
+    from dftbplus_gb300 import model as model_mod
+    sset = synth.make_skf_set([synth.SPECIES_O, synth.SPECIES_H], synth.WATER_SEED, synth.WATER_DRAW)
+    names = ["O", "H"]
+    for (a, b), d in sset.items():
+        h10, s10 = synth.skf_columns10(d)
+        homo = (d.onsite, d.hubbu, d.occ, d.mass) if a == b else None
+        skf.write_skf(str(tmp_path / f"{names[a]}-{names[b]}.skf"), d.dist, h10, s10, homo=homo,
+                      repulsive=d.repulsive)
+    fmt = str(tmp_path / "{A}-{B}.skf")
+    cache = str(tmp_path / "tables.npz")
+    sp = [synth.SPECIES_O, synth.SPECIES_H]
+    model_mod.Model.from_files(sp, fmt, cache=cache)
+    monkeypatch.setattr(model_mod, "CACHE_FORMAT", model_mod.CACHE_FORMAT + 1)
+    parsed = []
+    real_read = model_mod.read_skf
+    monkeypatch.setattr(model_mod, "read_skf", lambda *a, **k: parsed.append(a) or real_read(*a, **k))
+    model_mod.Model.from_files(sp, fmt, cache=cache)
+    assert parsed                                        # stale layout: reparsed
+    with np.load(cache) as z:
+        assert int(z["format"]) == model_mod.CACHE_FORMAT

@@ -58,3 +58,20 @@ def test_water_cluster_geometry():
         assert abs(ang - 104.5) < 1e-6
     c2, _ = synth.water_cluster(32, 10.0, 1)
     assert np.array_equal(c, c2)            # seeded: the same cluster every time
+
+
+def test_water_table_draw_criteria(water_model):
+    """The accepted water table draw: lambda_min(S) >= 0.2 on the (H2O)32 and (H2O)128 clusters and an
+    (H2O)32 SCC HOMO-LUMO gap above 0.1 Ha; the preceding draw 1 (the only other definite one) has a
+    gap below 0.1 Ha."""
+    from dftbplus_gb300 import synth
+    for n_mol, radius, seed in [(32, 10.0, 1), (128, 20.0, 128)]:
+        c, s = synth.water_cluster(n_mol, radius, seed)
+        _, S = O.build_h0_s(O.System(water_model, c, s))
+        assert np.linalg.eigvalsh(S)[0] >= 0.2
+    c, s = synth.water_cluster(32, 10.0, 1)
+    nocc = int(round(water_model.n_electrons(s) / 2))
+    res = O.run_scc(O.System(water_model, c, s))
+    assert res.converged and res.eig[nocc] - res.eig[nocc - 1] > 0.1
+    res1 = O.run_scc(O.System(synth.water_model(draw=1), c, s))
+    assert res1.eig[nocc] - res1.eig[nocc - 1] < 0.1
