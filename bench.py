@@ -38,8 +38,15 @@ KT, SCC_TOL, MIX = 1e-3, 1e-7, 0.2
 METRIC = "E+F evals/s, mixed vs FP64 on 1 GB300 at |dE|<=1e-6 Ha/atom"
 
 
+# the large spd system: anatase TiO2 sphere, 1,700 Ti + 3,400 O (Ti spd 9 + O sp 4 = 28,900 orbitals)
+TIO2_NTI = 1700
+
+
 def _workload(name):
     from dftbplus_gb300 import synth
+    if name == "tio2":
+        coords, species = synth.anatase_cluster(TIO2_NTI)
+        return synth.anatase_model(), coords, species
     n_mol, radius, seed = CONFIGS[name]
     coords, species = synth.water_cluster(n_mol, radius, seed)
     return synth.water_model(), coords, species
@@ -190,7 +197,18 @@ def gemm_peak(dtype_name="float64"):
 
 
 BF16_PEAK_FALLBACK = 1700.0
+HBM_PEAK_FALLBACK = 6800.0
 BF16_PEAK_SOURCE = "measured sustained cuBLAS bf16 GEMM (MEASURED_PEAKS.json bf16_tflops_sustained)"
+HBM_PEAK_SOURCE = "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+N_SM = 152
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def bf16_peak():
@@ -198,36 +216,132 @@ def bf16_peak():
     inside a seconds-long step), else the fallback of an earlier GB300 measurement."""
     global BF16_PEAK_SOURCE
     try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return float(json.load(f)["bf16_tflops_sustained"])
-    except (OSError, KeyError, ValueError):
+        return float(_measured_peaks()["bf16_tflops_sustained"])
+    except (KeyError, ValueError, TypeError):
         BF16_PEAK_SOURCE = "fallback: 1.7 PFLOP/s sustained bf16 of an earlier GB300 measurement"
         return BF16_PEAK_FALLBACK
 
 
-def cpu_scc_iteration_time(name, reps=1):
-    """Seconds of one SCC iteration of the CPU oracle at full size (H assembly, dsygvd, density
-    matrix, Mulliken, potentials), on all host cores."""
+def hbm_peak():
+    """HBM copy bandwidth of this GPU pool (GB/s): measured, else the fallback of an earlier GB300."""
+    global HBM_PEAK_SOURCE
+    try:
+        return float(_measured_peaks()["hbm_gbs"])
+    except (KeyError, ValueError, TypeError):
+        HBM_PEAK_SOURCE = "fallback: 6.8 TB/s of an earlier GB300 measurement"
+        return HBM_PEAK_FALLBACK
+
+
+def traffic_per_launch(kernel, workload):
+    """DRAM bytes per launch of a kernel from the committed ncu summary (profiles/traffic.json:
+    dram__bytes_read.sum + dram__bytes_write.sum of one capture, scaled to the workload there)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)[workload][kernel]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def kernel_classes(prof, steps, sm_mhz, dgemm_tflops, sgemm_tflops, workload):
+    """Per-step time and achieved rate of every timed kernel class of the evaluation, with the peak
+    its rate is held against: HBM-streaming kernels against the measured copy bandwidth, CUDA-core
+    FP32/FP64 work against SMs x lanes x clock (and the cuBLAS rate measured in the same run),
+    tensor-core products against the measured bf16 peak."""
+    f = (sm_mhz or 2070.0) * 1e6
+    fp32_cc = N_SM * 128 * 2 * f / 1e12          # FP32 FMA lanes per SM: 128
+    fp64_cc = N_SM * 2 * 2 * f / 1e12            # FP64 FMA per SM per clock: 2
+    hbm = hbm_peak()
+    bf16 = bf16_peak()
+    spec = {
+        "k_sytrd_panel": ("sytrd_panel_kernel (one-stage tridiagonalisation panels, FP64 and FP32)", "hbm",
+                          "GB/s", 1e-9, hbm, HBM_PEAK_SOURCE + " of measured"),
+        "k_panel_qr": ("panel_qr_kernel (two-stage band reduction, panel QR)", "hbm", "GB/s", 1e-9, hbm,
+                       HBM_PEAK_SOURCE + " of measured"),
+        "k_back_q2": ("q2_apply_kernel (bulge-chasing reflectors applied to the eigenvectors, FP32)", "fp32",
+                      "TFLOP/s", 1e-12, fp32_cc, f"FP32 CUDA cores {N_SM} SMs x 128 lanes x 2 x {f / 1e6:.0f} MHz"),
+        "k_chase": ("sb2st_kernel (bulge chasing, band -> tridiagonal)", "latency", "tasks/s", 1.0, None,
+                    "latency-bound chain of Householder tasks (no throughput peak)"),
+        "gemm_fp64": ("dgemm_kernel<double> (FP64 FMA GEMM launches)", "fp64", "TFLOP/s", 1e-12, fp64_cc,
+                      f"FP64 {N_SM} SMs x 2 FMA x 2 x {f / 1e6:.0f} MHz (cuBLAS DGEMM measured here: "
+                      f"{dgemm_tflops:.2f} TFLOP/s)"),
+        "gemm_fp32": ("dgemm_kernel<float>, sgemm128_kernel, tc_gemm_kernel (FP32-class GEMM launches)", "fp32",
+                      "TFLOP/s", 1e-12, fp32_cc, f"FP32 CUDA cores {N_SM} SMs x 128 lanes x 2 x {f / 1e6:.0f} MHz "
+                      f"(cuBLAS SGEMM measured here: {sgemm_tflops:.1f} TFLOP/s)"),
+        "gemm_tc_fp64": ("dg_gemm_kernel (FP64 products as 36 exact BF16 digit products on tcgen05)", "tensor",
+                         "TFLOP/s", 36e-12, bf16, BF16_PEAK_SOURCE + " of measured"),
+    }
+    out = {}
+    for key, (name, bound, unit, scale, peak, src) in spec.items():
+        v = prof.get(key)
+        if not v or v["ms"] <= 0:
+            continue
+        ms = v["ms"] / max(steps, 1)
+        launches = v["calls"] / max(steps, 1)
+        rate = v["flops"] * scale / (v["ms"] / 1e3)
+        tr = traffic_per_launch(name.split(" ")[0], workload)
+        out[key] = {"kernel": name, "bound": bound, "ms_per_step": ms, "launches_per_step": launches,
+                    "achieved": rate, "unit": unit, "peak": peak, "frac": (rate / peak) if peak else None,
+                    "peak_source": src, "traffic": tr,
+                    "work_per_launch": v["flops"] / max(v["calls"], 1)}
+    return out
+
+
+def _cpu_threads():
+    ncpu = os.cpu_count() or 1
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ.setdefault(v, str(ncpu))
+    return ncpu
+
+
+def cpu_full_evaluations(name, budget_s, max_evals):
+    """Complete CPU evaluations of the oracle on all host cores: H0/S, SCC from the neutral charges
+    to 1e-7 e with Broyden mixing, energies and gradients, one evaluation after another until
+    max_evals are done or the next one would pass budget_s. At least one is timed. A warm-up
+    evaluation of (H2O)32 (untimed) starts the BLAS threads first. Returns (seconds per evaluation
+    list, SCC iterations of the last one)."""
+    from oracle import dftb_oracle as O
+    model, coords, species = _workload(name)
+    wm, wc, ws = _workload("h2o32")
+    O.gradients(O.System(wm, wc, ws), O.run_scc(O.System(wm, wc, ws), kt=KT, scc_tol=SCC_TOL))
+    times, n_iter = [], 0
+    t_start = time.perf_counter()
+    while len(times) < max_evals:
+        t0 = time.perf_counter()
+        sys_ = O.System(model, coords, species)
+        ref = O.run_scc(sys_, kt=KT, scc_tol=SCC_TOL, mixer=O.BroydenMixer(alpha=MIX))
+        O.gradients(sys_, ref, kt=KT)
+        times.append(time.perf_counter() - t0)
+        n_iter = ref.n_iter
+        if time.perf_counter() - t_start + times[-1] > budget_s:
+            break
+    return times, n_iter
+
+
+def cpu_eval_sample(name):
+    """Bounded CPU sample (about 10-30 s at (H2O)1024 on 16 cores) of one complete oracle evaluation:
+    H0/S build, one SCC iteration (potentials, H, LAPACK dsygvd, Fermi filling, density matrix,
+    Mulliken, Broyden step) and the gradients, each timed; the evaluation is H0/S + n_iter SCC
+    iterations + gradients. Returns (seconds per evaluation, sample description)."""
     from oracle import dftb_oracle as O
     model, coords, species = _workload(name)
     sys_ = O.System(model, coords, species)
-    H0, S = O.build_h0_s(sys_)
-    es = O.Electrostatics(sys_)
-    n_el = model.n_electrons(sys_.species)
-    import scipy.linalg
-    times = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        dq = np.zeros(sys_.n_atom)
-        V = es.potential(dq)
-        Vo = V[sys_.atom_of_orb]
-        H = H0 + 0.5 * S * (Vo[:, None] + Vo[None, :])
-        eig, C = scipy.linalg.eigh(H, S, driver="gvd")
-        f, *_ = O.fermi_filling(eig, n_el, KT)
-        rho = O.density_matrix(C, f)
-        q = O.mulliken_orbital(rho, S)
-        times.append(time.perf_counter() - t0)
-    return float(np.median(times))
+    t0 = time.perf_counter()
+    H0S = O.build_h0_s(sys_)
+    t_h0s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref1 = O.run_scc(sys_, kt=KT, scc_tol=SCC_TOL, max_iter=1, H0S=H0S, mixer=O.BroydenMixer(alpha=MIX))
+    t_it = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.gradients(sys_, ref1, kt=KT)
+    t_grad = time.perf_counter() - t0
+    n_iter = REF_SCC_ITERS[name]
+    total = t_h0s + n_iter * t_it + t_grad
+    return total, (f"one complete oracle evaluation of {name} assembled from timed parts: H0/S build "
+                   f"{t_h0s:.1f} s, one SCC iteration {t_it:.1f} s (LAPACK dsygvd via OpenBLAS) x {n_iter} "
+                   f"iterations, gradients {t_grad:.1f} s")
+
+
+REF_BUDGET_S = 300.0    # wall-clock budget of the reference arm's timed evaluations
 
 
 def run_reference(args):
@@ -252,23 +366,18 @@ def run_reference(args):
                 "e2e": {"value": v, "unit": "molecules/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    ncpu = os.cpu_count() or 1
-    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
-        os.environ.setdefault(v, str(ncpu))
-    n_iter = REF_SCC_ITERS[args.config]
-    steps = []
-    for i in range(args.warmup + args.steps):
-        t = cpu_scc_iteration_time(args.config)
-        if i >= args.warmup:
-            steps.append(t)
-    t_iter = float(np.median(steps))
-    value = 1.0 / (t_iter * n_iter)
-    sample = (f"one SCC iteration (H assembly, LAPACK dsygvd, density matrix, Mulliken) of {args.config} "
-              f"per step, scaled by the {n_iter} SCC iterations this workload takes; gradients not timed")
+    ncpu = _cpu_threads()
+    times, n_iter = cpu_full_evaluations(args.config, REF_BUDGET_S, max(1, args.steps))
+    t_eval = float(np.mean(times))
+    value = 1.0 / t_eval
+    sample = (f"{len(times)} complete evaluation(s) of {args.config} timed one after another ({args.steps} "
+              f"requested; the {REF_BUDGET_S:.0f} s budget bounds the run): H0/S, SCC from the neutral "
+              f"charges to 1e-7 e ({n_iter} iterations, LAPACK dsygvd via OpenBLAS on {ncpu} threads), "
+              f"energies and gradients, after one untimed (H2O)32 warm-up evaluation")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * n_iter * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded water cluster, analytic SK tables)",
+            "steps": len(times), "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_eval * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded water cluster, analytic SK tables)",
             "config": {"workload": args.config, "orbitals": _norb(args.config), "kT": KT, "scc_tol": SCC_TOL},
             "cpu_baseline": {"value": value, "unit": "evals/s", "cores": ncpu, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -439,6 +548,8 @@ def run_batch(args):
 
 
 def _norb(name):
+    if name == "tio2":
+        return 9 * TIO2_NTI + 4 * 2 * TIO2_NTI
     return CONFIGS[name][0] * 6
 
 
@@ -533,7 +644,9 @@ def run_gpu(args):
                 "accuracy_vs_fp64": {"dE_per_atom": abs(e_main - r64["energies"]["EMermin"]) / N,
                                      "max_dF": float(np.max(np.abs(g_main - g64)))}}
 
-    # e2e through the public API with host buffers
+    # e2e through the public API with host buffers (the first context is released first: at the
+    # large configuration two contexts would not fit the device together)
+    ctx.close()
     calc = binding.DftbGpu(model, coords, species, kT=KT, scc_tol=SCC_TOL, mixing=MIX, device=dev, precision=prec)
     calc.get_energy(); calc.get_gradients()
     barrier()
@@ -557,43 +670,30 @@ def run_gpu(args):
 
     if rank != 0:
         return
-    # roofline of the dominant GEMM class: FP64 FMA and FP32 FMA GEMMs against the library GEMM rate
-    # measured now, the tensor-core FP64 digit-slice products (36 BF16 products per FP64 product)
-    # against the measured sustained BF16 tensor peak
-    classes = {"fp64": prof["gemm_fp64"], "fp32": prof["gemm_fp32"], "tc_fp64": prof["gemm_tc_fp64"]}
-    dom = max(classes, key=lambda k: classes[k]["ms"])
-    use32 = dom == "fp32"
-    g = classes[dom]
-    peak = gemm_peak("float32") if use32 else (bf16_peak() if dom == "tc_fp64" else gemm_peak("float64"))
-    peak64 = gemm_peak("float64") if dom != "fp64" else peak
+    # per-kernel classes of the evaluation; the roofline is the one that takes the most time
+    dgemm_tf = gemm_peak("float64")
+    sgemm_tf = gemm_peak("float32")
+    clocks = clk.summary()
+    kc = kernel_classes(prof, args.steps, clocks.get("sm_mhz"), dgemm_tf, sgemm_tf, args.config)
+    dom = max(kc, key=lambda k: kc[k]["ms_per_step"]) if kc else None
     cpu = None
     if not args.no_cpu_baseline:
-        ncpu = os.cpu_count() or 1
-        t_it = cpu_scc_iteration_time(args.config)
-        n_cpu = fp64["scc_iterations"] if fp64 else n_iter   # the CPU path is plain FP64
-        cpu = {"value": 1.0 / (t_it * n_cpu), "unit": "evals/s", "cores": ncpu, "kind": "port",
-               "sample": f"one SCC iteration of the CPU oracle (LAPACK dsygvd via OpenBLAS, {ncpu} threads) "
-                         f"of {args.config} scaled by the {n_cpu} SCC iterations of the FP64 cycle; "
-                         f"gradients not timed"}
+        ncpu = _cpu_threads()
+        t_eval, sample = cpu_eval_sample(args.config)
+        cpu = {"value": 1.0 / t_eval, "unit": "evals/s", "cores": ncpu, "kind": "port", "sample": sample}
     # the batched workload (second half of the headline metric), measured on the same GPU
     batched = None
     if not args.no_batch and world == 1:
         bout, be2e, bseq, bmols = batch_measure(dev)
         bcpu = None if args.no_cpu_baseline else cpu_batch_rate(bmols)
-        batched = _batch_summary(bout, be2e, bseq, bcpu, peak64)
-    tc_mult = 36.0 if dom == "tc_fp64" else 1.0
-    achieved = tc_mult * g["flops"] / (g["ms"] / 1e3) / 1e12 if g["ms"] > 0 else 0.0
-    gemm_classes = {k: {"ms_per_step": v["ms"] / max(args.steps, 1), "calls_per_step": v["calls"] / max(args.steps, 1),
-                        "fp64_equivalent_tflops": (v["flops"] / (v["ms"] / 1e3) / 1e12) if v["ms"] > 0 else None}
-                    for k, v in classes.items()}
-    kernels = {"fp64": "dgemm_kernel<double> (all FP64 GEMM launches)",
-               "fp32": "dgemm_kernel<float> and sgemm128_kernel (FP32 FMA GEMM launches)",
-               "tc_fp64": "dg_gemm_kernel (FP64 products as 36 exact BF16 digit products on tcgen05, "
-                          "with their two packing launches)"}
-    peak_src = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run (no FP64 entry in the measured peaks)",
-                "fp32": "cuBLAS SGEMM (TF32 off) 8192^3 measured in this run (no FP32 entry in the measured peaks)",
-                "tc_fp64": BF16_PEAK_SOURCE}
+        batched = _batch_summary(bout, be2e, bseq, bcpu, dgemm_tf)
     phases = {k: round(v["ms"] / max(args.steps, 1), 2) for k, v in prof.items()}
+    roof = None
+    if dom is not None:
+        d = kc[dom]
+        roof = {"bound": d["bound"], "kernel": d["kernel"], "achieved": d["achieved"], "peak": d["peak"],
+                "unit": d["unit"], "frac": d["frac"], "peak_source": d["peak_source"], "traffic": d["traffic"],
+                "ms_per_step": d["ms_per_step"], "share_of_step": d["ms_per_step"] / (t_dev / args.steps * 1e3)}
 
     expected_iters = REF_SCC_ITERS.get(args.config)
     line = {"metric": METRIC, "precision": args.precision, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -605,16 +705,11 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": world * args.steps / t_e2e, "unit": "evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "tensor" if dom == "tc_fp64" else dom,
-                         "kernel": kernels[dom],
-                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None,
-                         "peak_source": peak_src[dom],
-                         "traffic": None},
-            "gemm_classes": gemm_classes,
+            "roofline": roof,
+            "kernel_classes": kc,
             "fp64": fp64,
             "batched": batched,
-            "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk.summary(),
+            "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "phases_ms_per_step": phases, "scc_iterations_by_kind": by_kind, "wall_s": wall,
             "energy": info["energies"]["EMermin"]}
     n_iter64 = fp64["scc_iterations"] if fp64 else n_iter   # the recorded count is the FP64 cycle's
@@ -629,7 +724,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="h2o1024", choices=sorted(CONFIGS) + ["batch4096"])
+    ap.add_argument("--config", default="h2o1024", choices=sorted(CONFIGS) + ["batch4096", "tio2"])
     ap.add_argument("--no-batch", action="store_true", help="leave the batched workload out of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])

@@ -74,6 +74,8 @@ SIGNATURES = {
                                      _dp, _dp, C.c_double, _dp, C.c_int]),
     "dftbgpu_set_tensor_cores": (C.c_int, [C.c_int]),
     "dftbgpu_set_fp64_emulation": (C.c_int, [C.c_int]),
+    "dftbgpu_set_two_stage": (C.c_int, [C.c_int]),
+    "dftbgpu_test_twostage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_sgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
                                      C.POINTER(C.c_float), C.c_int, C.c_int]),
@@ -91,7 +93,7 @@ SIGNATURES = {
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
           "density", "mulliken_energy", "broyden", "gradients", "perturbation", "gemm_fp64", "gemm_fp32",
-          "gemm_tc_fp64"]
+          "gemm_tc_fp64", "k_sytrd_panel", "k_panel_qr", "k_chase", "k_back_q2"]
 
 _lib = None
 
@@ -237,6 +239,16 @@ class Context:
         self.check(self.lib.dftbgpu_test_tridiag(self.h, n, _p(A, C.c_double), _p(d, C.c_double), _p(e, C.c_double)))
         return d, e[:n - 1]
 
+    def test_twostage(self, a, fp32=False):
+        """Two-stage reduction of the symmetric a: (d, e, q) with a = q tridiag(d, e) q^T."""
+        n = a.shape[0]
+        A = np.asfortranarray(a, dtype=np.float64)
+        d = np.zeros(n); e = np.zeros(max(n - 1, 1))
+        q = np.zeros((n, n), order="F")
+        self.check(self.lib.dftbgpu_test_twostage(self.h, n, _p(A, C.c_double), 1 if fp32 else 0, _p(d, C.c_double),
+                                                  _p(e, C.c_double), _p(q, C.c_double)))
+        return d, e[:n - 1], q
+
     def test_stedc(self, d, e):
         n = len(d)
         dd = np.array(d, dtype=np.float64); ee = np.zeros(max(n - 1, 1)); ee[:n - 1] = e
@@ -375,6 +387,17 @@ def set_fp64_emulation(enable: bool) -> bool:
     """Run the mixed form's FP64 products as exact BF16 digit-slice products on the tensor cores
     (process-wide, on by default); returns the previous setting."""
     return bool(load_library().dftbgpu_set_fp64_emulation(1 if enable else 0))
+
+
+def set_two_stage(mode) -> int:
+    """Reduction of the FP32 eigensolves of the mixed form (process-wide): 0 / False one-stage,
+    1 / True two-stage (band, then bulge chasing), 2 automatic by size (the default). Returns the
+    previous mode."""
+    m = int(mode)
+    prev = load_library().dftbgpu_set_two_stage(m)
+    if prev < 0:
+        raise ValueError(f"two-stage mode {mode!r}: expected 0, 1 or 2")
+    return prev
 
 
 def default_opts(**kw) -> SccOpts:

@@ -10,6 +10,7 @@
 #include "batch.cuh"
 #include "dftb_kernels.cuh"
 #include "linalg.cuh"
+#include "twostage.cuh"
 
 namespace dg {
 
@@ -55,7 +56,9 @@ struct Ctx {
   size_t cap_n32 = 0;
   float *L32 = nullptr, *Li32 = nullptr, *A0_32 = nullptr, *A32 = nullptr, *T32 = nullptr, *V32 = nullptr,
         *Z32 = nullptr, *C32 = nullptr, *d32 = nullptr, *e32 = nullptr, *tau32 = nullptr, *wk32_sytrd = nullptr,
-        *wk32_ormtr = nullptr, *wk32_stedc = nullptr;
+        *wk32_ormtr = nullptr, *wk32_stedc = nullptr, *wk32_ts = nullptr;
+  double *wk_ts = nullptr;   // FP64 two-stage workspace (stage-level test hook)
+  size_t cap_ts64 = 0;
   bool mixed_ready = false;
   int mixed_iters = 0;    // FP32 iterations of the last SCC call
   bool scc_mixed = false; // the last SCC call ran the mixed form
@@ -280,8 +283,8 @@ static int ensure_broyden(Ctx *c, int natom, int max_iter) {
   return DFTBGPU_OK;
 }
 
-// FP32 copies of L, L^-1 and A0 for the reduced-precision iterations (once per geometry).
-static int ensure_mixed(Ctx *c, int n) {
+// FP32 buffers of the reduced-precision eigensolves.
+static int ensure_mixed_buffers(Ctx *c, int n) {
   if ((size_t)n > c->cap_n32) {
     size_t nn = (size_t)n * n;
     for (float **p : {&c->L32, &c->Li32, &c->A0_32, &c->A32, &c->T32, &c->V32, &c->Z32, &c->C32})
@@ -290,9 +293,16 @@ static int ensure_mixed(Ctx *c, int n) {
     DG_CHECK(c, dev_alloc(c, &c->wk32_sytrd, sytrd_work_size<float>(n)));
     DG_CHECK(c, dev_alloc(c, &c->wk32_ormtr, ormtr_work_size<float>(n, n)));
     DG_CHECK(c, dev_alloc(c, &c->wk32_stedc, stedc_work_size(n)));
+    DG_CHECK(c, dev_alloc(c, &c->wk32_ts, twostage_work_size<float>(n)));
     c->cap_n32 = n;
     c->mixed_ready = false;
   }
+  return DFTBGPU_OK;
+}
+
+// FP32 copies of L, L^-1 and A0 for the reduced-precision iterations (once per geometry).
+static int ensure_mixed(Ctx *c, int n) {
+  DG_CHECK(c, ensure_mixed_buffers(c, n));
   // size the tensor-core FP64 scratch once; if the device cannot hold it, the FP64 products of the
   // mixed form stay on FP64 FMA (gemm<double> falls back per product)
   if (g_tc_dgemm_mixed) tc_dgemm_reserve(n, n, n);
@@ -319,6 +329,20 @@ static int ensure_pert(Ctx *c, int n, int natom) {
     c->cap_pert_atoms = natom;
   }
   return DFTBGPU_OK;
+}
+
+template <typename T>
+__global__ void identity_kernel(int n, T *Z) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) Z[i + i * (long long)n] = T(1);
+}
+static void identity_f(cudaStream_t s, int n, float *Z) {
+  identity_kernel<float><<<ceil_div(n, 256), 256, 0, s>>>(n, Z);
+  count_launch();
+}
+static void identity_d(cudaStream_t s, int n, double *Z) {
+  identity_kernel<double><<<ceil_div(n, 256), 256, 0, s>>>(n, Z);
+  count_launch();
 }
 
 static ModelDev model_view(Ctx *c) { return ModelDev{c->nsp, c->d_sp, c->d_pair, c->d_tab, c->d_rep}; }
@@ -453,7 +477,7 @@ int dftbgpu_destroy(dftbgpu_ctx *c) {
                   c->wk_ormtr, c->wk_stedc, c->iwk_stedc, c->d_status, c->d_scal, c->bro.ww, c->bro.aa,
                   c->bro.dF, c->bro.uu, c->bro.qlast, c->bro.dlast, c->L32, c->Li32, c->A0_32, c->A32,
                   c->T32, c->V32, c->Z32, c->C32, c->d32, c->e32, c->tau32, c->wk32_sytrd, c->wk32_ormtr,
-                  c->wk32_stedc, c->Mt32, c->Zp32, c->rho_ref, c->Vref};
+                  c->wk32_stedc, c->Mt32, c->Zp32, c->rho_ref, c->Vref, c->wk32_ts, c->wk_ts};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (c->batch) {
@@ -753,7 +777,11 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       gemm<float>(s, 'N', 'N', n, n, n, 1.f, c->Li32, n, c->T32, n, 0.f, c->C32, n, kALower | kBLower | kCLower);
       add_half_lower_f(s, n, c->A0_32, c->C32, c->A32);
       mark(c, kPhSytrd);
-      sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd, c->d_status);
+      const bool two_stage = use_twostage(n);
+      if (two_stage)
+        twostage_reduce<float>(s, n, c->A32, n, c->d32, c->e32, c->V32, n, c->wk32_ts, c->d_status);
+      else
+        sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd, c->d_status);
       mark(c, kPhStedc);
       if (stedc<float>(s, n, c->d32, c->e32, c->Z32, n, c->wk32_stedc, c->iwk_stedc, c->d_status) != 0)
         return set_error(c, DFTBGPU_ERR_ARGS, "stedc workspace layout error");
@@ -762,7 +790,10 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
       DG_CHECK(c, pick(&k));
       mark(c, kPhBack);
       if (k > 0) {
-        ormtr_left<float>(s, n, k, c->V32, n, c->tau32, c->Z32, n, c->wk32_ormtr);
+        if (two_stage)
+          twostage_back<float>(s, n, k, c->Z32, n, c->V32, n, c->wk32_ts, c->d_status);
+        else
+          ormtr_left<float>(s, n, k, c->V32, n, c->tau32, c->Z32, n, c->wk32_ormtr);
         gemm<float>(s, 'T', 'N', n, k, n, 1.f, c->Li32, n, c->Z32, n, 0.f, c->C32, n, kAUpper);
       }
       mark(c, kPhDensity);
@@ -962,6 +993,11 @@ int dftbgpu_set_tensor_cores(int enable) {
   const int prev = g_tc_gemm ? 1 : 0;
   g_tc_gemm = enable != 0;
   return prev;
+}
+
+int dftbgpu_set_two_stage(int mode) {
+  if (mode < 0 || mode > 2) return -1;
+  return g_twostage.exchange(mode);
 }
 
 int dftbgpu_set_fp64_emulation(int enable) {
@@ -1175,6 +1211,46 @@ int dftbgpu_test_tridiag(dftbgpu_ctx *c, int n, const double *a, double *d, doub
   if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
   c->have_geom = false;
   c->have_scc = false;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_test_twostage(dftbgpu_ctx *c, int n, const double *a, int fp32, double *d, double *e, double *q) {
+  if (!c || !a || !d || !e || !q || n <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const size_t nn = (size_t)n * n;
+  DG_CHECK(c, ensure_orbitals(c, n));
+  DG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  DG_CUDA(c, cudaMemcpyAsync(c->H, a, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  if (fp32) {
+    DG_CHECK(c, ensure_mixed_buffers(c, n));
+    convert_d2f(s, nn, c->H, c->A32);
+    twostage_reduce<float>(s, n, c->A32, n, c->d32, c->e32, c->V32, n, c->wk32_ts, c->d_status);
+    // Q = Q1 Q2 applied to the identity
+    set_zero_t<float>(s, c->Z32, nn);
+    identity_f(s, n, c->Z32);
+    twostage_back<float>(s, n, n, c->Z32, n, c->V32, n, c->wk32_ts, c->d_status);
+    convert_f2d(s, n, c->d32, c->dd);
+    if (n > 1) convert_f2d(s, n - 1, c->e32, c->ee);
+    convert_f2d(s, nn, c->Z32, c->Z);
+  } else {
+    const size_t need = twostage_work_size<double>(n);
+    if (need > c->cap_ts64) {
+      DG_CHECK(c, dev_alloc(c, &c->wk_ts, need));
+      c->cap_ts64 = need;
+    }
+    twostage_reduce<double>(s, n, c->H, n, c->dd, c->ee, c->Vh, n, c->wk_ts, c->d_status);
+    set_zero(s, c->Z, nn);
+    identity_d(s, n, c->Z);
+    twostage_back<double>(s, n, n, c->Z, n, c->Vh, n, c->wk_ts, c->d_status);
+  }
+  DG_CHECK(c, check_status(c, "two-stage reduction"));
+  DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
+  DG_CUDA(c, cudaMemcpy(q, c->Z, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  c->have_geom = false;
+  c->have_scc = false;
+  c->mixed_ready = false;
   return DFTBGPU_OK;
 }
 

@@ -68,7 +68,10 @@ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 // Profiling phases (order documented in include/dftbgpu.h, dftbgpu_profile_enable).
 enum Phase : int {
   kPhH0S = 0, kPhPot, kPhTransform, kPhSytrd, kPhStedc, kPhFermi, kPhBack, kPhDensity, kPhMulliken,
-  kPhBroyden, kPhForces, kPhPert, kPhGemm, kPhGemm32, kPhGemmTc, kNPhase
+  kPhBroyden, kPhForces, kPhPert, kPhGemm, kPhGemm32, kPhGemmTc,
+  // single kernels, timed launch by launch (work = algorithmic bytes or tasks, see the header)
+  kPhKSytrdPanel, kPhKPanelQr, kPhKChase, kPhKBackQ2,
+  kNPhase
 };
 
 // Device-side status word codes (written by bounded device loops instead of spinning/trapping).

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "gridsync.cuh"
 #include "linalg.cuh"
 
 namespace dg {
@@ -611,68 +612,6 @@ void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int
 constexpr int PB = 32;
 constexpr int ST = 64;                 // symv tile
 constexpr int kMaxPanelCtas = 4096;    // partial-sum slots per reduction
-constexpr unsigned kBarrierSpinLimit = 1u << 24;   // ~1.5 s of polling before a barrier gives up
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-template <int NT, typename T>
-__device__ T block_sum(T v, T *sh) {
-  v = warp_sum(v);
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  T r = T(0);
-  if (threadIdx.x < 32) {
-    r = (threadIdx.x < NT / 32) ? sh[threadIdx.x] : T(0);
-    r = warp_sum(r);
-    if (threadIdx.x == 0) sh[0] = r;
-  }
-  __syncthreads();
-  r = sh[0];
-  __syncthreads();
-  return r;
-}
-
-// Grid barrier state, zeroed once per reduction: a monotonic arrival counter (barrier number e of
-// the reduction completes when count reaches (e + 1) * CTAs) and an error word.
-struct GridBar {
-  unsigned count, pad0;
-  int err, pad1;
-};
-
-// Grid barrier for a cooperative launch (all CTAs co-resident): one atomic arrival per CTA, then
-// poll until every CTA of this barrier number has arrived. Bounded: after kBarrierSpinLimit polls
-// it records an error and stops waiting; once an error is recorded no barrier waits any more, so a
-// broken launch ends quickly with the error set.
-__device__ __forceinline__ void grid_sync(GridBar *b, unsigned nb, unsigned &epoch) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile int *verr = &b->err;
-    if (*verr == 0) {
-      __threadfence();
-      atomicAdd(&b->count, 1u);
-      const unsigned target = (epoch + 1u) * nb;
-      volatile unsigned *vc = &b->count;
-      unsigned it = 0;
-      while ((int)(*vc - target) < 0) {
-        if (++it > kBarrierSpinLimit) {
-          atomicExch(&b->err, 1);
-          break;
-        }
-        __nanosleep(20);
-      }
-      __threadfence();
-    }
-  }
-  ++epoch;
-  __syncthreads();
-}
-
 template <typename T>
 struct PanelArgs {
   T *A;
@@ -1040,8 +979,16 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
     PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, dpart, V, d, e, tau, bar, epoch0, status};
     epoch0 += 3u * (unsigned)nbp;
     void *args[] = {&pa};
+    KernelTimer kt(s);
     cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
     count_launch();
+    // algorithmic bytes: the lower triangle of A22 streamed once per column of the panel
+    double bytes = 0.0;
+    for (int jj = 0; jj < nbp; ++jj) {
+      const double m = (double)(n - (p0 + jj) - 1);
+      bytes += 0.5 * m * (m + 1.0) * sizeof(T);
+    }
+    kt.done(kPhKSytrdPanel, bytes);
     int t0 = p0 + nbp;
     int m2 = n - t0;
     if (m2 > 0) {
@@ -1079,6 +1026,14 @@ __global__ void larft_kernel(int nb, const T *G, const T *tau, T *Tf) {
   }
   for (int k = tid; k < nb * nb; k += blockDim.x) Tf[k] = t[k % nb][k / nb];
 }
+
+template <typename T>
+void larft(cudaStream_t s, int nb, const T *G, const T *tau, T *Tf) {
+  larft_kernel<T><<<1, OB, 0, s>>>(nb, G, tau, Tf);
+  count_launch();
+}
+template void larft<float>(cudaStream_t, int, const float *, const float *, float *);
+template void larft<double>(cudaStream_t, int, const double *, const double *, double *);
 
 template <typename T>
 size_t ormtr_work_size(int n, int k) {

@@ -65,6 +65,33 @@ struct GemmProfile {
 };
 extern thread_local GemmProfile g_gemm_prof;   // per calling thread (its context's profiler)
 
+// Events around one launch of a kernel that has its own profiler phase (kPhK*); work is the
+// launch's algorithmic work in that phase's unit. Inactive while profiling is off or the stream is
+// being captured.
+struct KernelTimer {
+  cudaEvent_t e0 = nullptr;
+  cudaStream_t s = nullptr;
+  explicit KernelTimer(cudaStream_t st) : s(st) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cap);
+    if (g_gemm_prof.on && cap == cudaStreamCaptureStatusNone) {
+      cudaEventCreate(&e0);
+      cudaEventRecord(e0, s);
+    }
+  }
+  void done(int phase, double work) {
+    if (!e0) return;
+    cudaEvent_t e1;
+    cudaEventCreate(&e1);
+    cudaEventRecord(e1, s);
+    g_gemm_prof.ev.push_back(e0);
+    g_gemm_prof.ev.push_back(e1);
+    g_gemm_prof.flops.push_back(work);
+    g_gemm_prof.phase.push_back(phase);
+    e0 = nullptr;
+  }
+};
+
 // In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
 void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);
 
@@ -89,6 +116,11 @@ template <typename T>
 size_t ormtr_work_size(int n, int k);
 template <typename T>
 void ormtr_left(cudaStream_t s, int n, int k, const T *V, int ldv, const T *tau, T *Z, int ldz, T *work);
+
+// T (nb x nb, upper, leading dimension nb) of the compact WY form H_0 .. H_{nb-1} = I - V T V^T from
+// G = V^T V (nb x nb) and tau[nb]; nb <= 64.
+template <typename T>
+void larft(cudaStream_t s, int nb, const T *G, const T *tau, T *Tf);
 
 // Symmetric tridiagonal eigensolver (divide and conquer): d[n] (in: diagonal, out: eigenvalues
 // ascending), e[n-1] off-diagonal (read only); Q (n x n, ldq = n) eigenvectors.

@@ -208,9 +208,13 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  *   perturbation (mixed form: reference set-up and perturbative updates), 12 FP64 GEMM (all FP64
  *   GEMM launches, overlapping the phases above), 13 FP32 GEMM (mixed form, likewise), 14 FP64
  *   GEMM as tensor-core digit-slice products (mixed form, likewise; FLOPs counted as the FP64
- *   product's 2mnk, the tensor cores execute 36 BF16 products of it).
- * enable: 1 resets and starts accumulating, 0 stops. read: ms[15], flops[15] (algorithmic FLOPs
- * per phase as counted for the roofline), calls[15]; returns the number of phases written.
+ *   product's 2mnk, the tensor cores execute 36 BF16 products of it). Single kernels, timed launch
+ *   by launch (overlapping the phases above; "flops" holds the work in the unit given): 15 one-stage
+ *   tridiagonalisation panel kernel (algorithmic bytes: the trailing lower triangle once per
+ *   column), 16 two-stage panel QR (bytes: the panel read and written once), 17 bulge chasing
+ *   (Householder tasks), 18 two-stage back-transformation of the band stage (FLOPs 2 n^2 k).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[19], flops[19] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[19]; returns the number of phases written.
  */
 int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);
@@ -257,6 +261,16 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k
  * product on host arrays (column-major, flags as the library's triangular GEMM hints).
  */
 int dftbgpu_set_fp64_emulation(int enable);
+/*
+ * Two-stage reduction for the FP32 eigensolves of the mixed form (no reference counterpart; the
+ * reference reaches two-stage reductions through ELPA, elecsolvers/elecsolvertypes.F90:27, and
+ * MAGMA's dsygvd_m, math/eigensolver.F90:1143-1245): the matrix is reduced to a band of width 32 with
+ * GEMM-based panel updates, the band is chased to tridiagonal form in one persistent kernel, and the
+ * eigenvectors are back-transformed through both stages. mode 0: always the one-stage panel
+ * tridiagonalisation; 1: always two-stage; 2 (the default): two-stage from 12,000 orbitals on.
+ * Process-wide; returns the previous mode, or -1 for an invalid mode (nothing changes).
+ */
+int dftbgpu_set_two_stage(int mode);
 int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                           int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
 /*
@@ -274,6 +288,9 @@ int dftbgpu_test_dgemm(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, 
                        const double *a, const double *b, double beta, double *c, int flags);
 int dftbgpu_test_tridiag(dftbgpu_ctx *ctx, int n, const double *a, double *d, double *e);
 int dftbgpu_test_stedc(dftbgpu_ctx *ctx, int n, double *d, const double *e, double *q);
+/*   twostage: two-stage reduction of the symmetric a (n x n) in FP32 (fp32 = 1) or FP64 -> d[n],
+ *            e[n-1] and q[n*n] = Q1 Q2 (the accumulated transformation, a = q T q^T). */
+int dftbgpu_test_twostage(dftbgpu_ctx *ctx, int n, const double *a, int fp32, double *d, double *e, double *q);
 
 #ifdef __cplusplus
 }
