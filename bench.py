@@ -216,9 +216,11 @@ def bf16_peak():
     inside a seconds-long step), else the fallback of an earlier GB300 measurement."""
     global BF16_PEAK_SOURCE
     try:
-        return float(_measured_peaks()["bf16_tflops_sustained"])
+        v = float(_measured_peaks()["bf16_tflops_sustained"])
+        BF16_PEAK_SOURCE = "of measured: sustained cuBLAS bf16 GEMM (MEASURED_PEAKS.json bf16_tflops_sustained)"
+        return v
     except (KeyError, ValueError, TypeError):
-        BF16_PEAK_SOURCE = "fallback: 1.7 PFLOP/s sustained bf16 of an earlier GB300 measurement"
+        BF16_PEAK_SOURCE = "of fallback: 1.7 PFLOP/s sustained bf16 of an earlier GB300 measurement"
         return BF16_PEAK_FALLBACK
 
 
@@ -226,9 +228,11 @@ def hbm_peak():
     """HBM copy bandwidth of this GPU pool (GB/s): measured, else the fallback of an earlier GB300."""
     global HBM_PEAK_SOURCE
     try:
-        return float(_measured_peaks()["hbm_gbs"])
+        v = float(_measured_peaks()["hbm_gbs"])
+        HBM_PEAK_SOURCE = "of measured: copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+        return v
     except (KeyError, ValueError, TypeError):
-        HBM_PEAK_SOURCE = "fallback: 6.8 TB/s of an earlier GB300 measurement"
+        HBM_PEAK_SOURCE = "of fallback: 6.8 TB/s of an earlier GB300 measurement"
         return HBM_PEAK_FALLBACK
 
 
@@ -253,10 +257,15 @@ def kernel_classes(prof, steps, sm_mhz, dgemm_tflops, sgemm_tflops, workload):
     hbm = hbm_peak()
     bf16 = bf16_peak()
     spec = {
-        "k_sytrd_panel": ("sytrd_panel_kernel (one-stage tridiagonalisation panels, FP64 and FP32)", "hbm",
-                          "GB/s", 1e-9, hbm, HBM_PEAK_SOURCE + " of measured"),
+        "k_sytrd_panel": ("sytrd_panel_kernel<double> (one-stage tridiagonalisation panels, FP64: symmetric "
+                          "matrix-vector products 2 m^2 per column)", "fp64", "TFLOP/s", 1e-12, fp64_cc,
+                          f"FP64 {N_SM} SMs x 2 FMA x 2 x {f / 1e6:.0f} MHz (cuBLAS DGEMM measured here: "
+                          f"{dgemm_tflops:.2f} TFLOP/s)"),
+        "k_sytrd_panel32": ("sytrd_panel_kernel<float> (one-stage tridiagonalisation panels, FP32: trailing lower "
+                            "triangle streamed once per column)", "hbm", "GB/s", 1e-9, hbm,
+                            HBM_PEAK_SOURCE),
         "k_panel_qr": ("panel_qr_kernel (two-stage band reduction, panel QR)", "hbm", "GB/s", 1e-9, hbm,
-                       HBM_PEAK_SOURCE + " of measured"),
+                       HBM_PEAK_SOURCE),
         "k_back_q2": ("q2_apply_kernel (bulge-chasing reflectors applied to the eigenvectors, FP32)", "fp32",
                       "TFLOP/s", 1e-12, fp32_cc, f"FP32 CUDA cores {N_SM} SMs x 128 lanes x 2 x {f / 1e6:.0f} MHz"),
         "k_chase": ("sb2st_kernel (bulge chasing, band -> tridiagonal)", "latency", "tasks/s", 1.0, None,
@@ -268,7 +277,7 @@ def kernel_classes(prof, steps, sm_mhz, dgemm_tflops, sgemm_tflops, workload):
                       "TFLOP/s", 1e-12, fp32_cc, f"FP32 CUDA cores {N_SM} SMs x 128 lanes x 2 x {f / 1e6:.0f} MHz "
                       f"(cuBLAS SGEMM measured here: {sgemm_tflops:.1f} TFLOP/s)"),
         "gemm_tc_fp64": ("dg_gemm_kernel (FP64 products as 36 exact BF16 digit products on tcgen05)", "tensor",
-                         "TFLOP/s", 36e-12, bf16, BF16_PEAK_SOURCE + " of measured"),
+                         "TFLOP/s", 36e-12, bf16, BF16_PEAK_SOURCE),
     }
     out = {}
     for key, (name, bound, unit, scale, peak, src) in spec.items():
@@ -718,6 +727,85 @@ def run_gpu(args):
     print(json.dumps(line))
 
 
+def run_per_iteration(args):
+    """For a configuration whose plain FP64 evaluation is too long to time whole (the TiO2 sphere:
+    about 110 s per FP64 SCC iteration): geometry set-up, two FP64 SCC iterations, one iteration of
+    each kind of the mixed form (FP32 eigensolve, FP64-class eigensolve, perturbative update) and
+    the gradients of both forms, each timed; then both forms to convergence on smaller spheres of the
+    same model (40 and 100 Ti) for their iteration counts and energy agreement. One JSON line; the
+    evaluation-time model it prints (set-up + counts x per-iteration costs + gradients) is labelled
+    as such."""
+    from dftbplus_gb300 import binding, synth
+    rank, _, _ = _dist_env()
+    if rank != 0:
+        return
+    mix = args.mix_alpha
+
+    def run(ctx, **kw):
+        t0 = time.perf_counter()
+        r = ctx.scc(binding.default_opts(kT=KT, scc_tol=SCC_TOL, mix_alpha=mix, **kw))
+        t_scc = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ctx.gradients()
+        t_grad = time.perf_counter() - t0
+        h = ctx.scc_history()
+        return r, {"scc_s": t_scc, "grad_s": t_grad, "kinds": h["precision"].tolist(),
+                   "iter_s": [round(x / 1e3, 3) for x in h["ms"].tolist()]}
+
+    model, c, s = _workload(args.config)
+    ctx = binding.Context(0)
+    ctx.set_model(model)
+    t0 = time.perf_counter()
+    ctx.set_geometry(c, s)
+    t_geom = time.perf_counter() - t0
+    _, fp64 = run(ctx, precision=binding.PREC_FP64, max_iter=2)
+    # FP32 eigensolve, then (switch tolerance above any error) FP64-class, perturbative, perturbative, FP64-class
+    _, mixed = run(ctx, precision=binding.PREC_MIXED, max_iter=5, mixed_switch_tol=1e3)
+    norb = ctx.norb
+    ctx.close()
+    kinds = {binding.PREC_MIXED: "fp32", binding.PREC_FP64: "fp64_class", binding.ITER_PERTURB: "perturbative"}
+    per = {}
+    for k, t in zip(mixed["kinds"], mixed["iter_s"]):
+        per.setdefault(kinds[k], t)
+    t_fp64_iter = fp64["iter_s"][-1]
+    counts = []
+    if args.config == "tio2":
+        for nti in (40, 100):
+            cc, ss = synth.anatase_cluster(nti)
+            cx = binding.Context(0)
+            cx.set_model(model)
+            cx.set_geometry(cc, ss)
+            row = {"ti": nti, "orbitals": cx.norb}
+            for name, prec in (("fp64", binding.PREC_FP64), ("mixed", binding.PREC_MIXED)):
+                r, info = run(cx, precision=prec, max_iter=150)
+                kk = info["kinds"]
+                row[name] = {"converged": bool(r["converged"]), "iterations": len(kk),
+                             "by_kind": {kinds[k]: kk.count(k) for k in sorted(set(kk))},
+                             "EMermin": r["energies"]["EMermin"]}
+            row["dE_per_atom"] = abs(row["fp64"]["EMermin"] - row["mixed"]["EMermin"]) / len(ss)
+            counts.append(row)
+            cx.close()
+    model_eval = None
+    conv = [r for r in counts if r["fp64"]["converged"] and r["mixed"]["converged"]]
+    if conv:
+        big = conv[-1]
+        n64 = big["fp64"]["iterations"]
+        bk = big["mixed"]["by_kind"]
+        t64 = t_geom + fp64["iter_s"][0] + (n64 - 1) * t_fp64_iter + fp64["grad_s"]
+        tmx = (t_geom + bk.get("fp32", 0) * per["fp32"] + bk.get("fp64_class", 0) * per["fp64_class"]
+               + bk.get("perturbative", 0) * per["perturbative"] + mixed["grad_s"])
+        model_eval = {"basis": f"iteration counts of the converged {big['ti']}-Ti sphere x per-iteration costs "
+                               f"measured at full size (a model, not a timed evaluation)",
+                      "fp64_s": t64, "mixed_s": tmx, "mixed_vs_fp64": t64 / tmx}
+    line = {"mode": "per-iteration", "config": {"workload": args.config, "orbitals": norb, "kT": KT,
+                                                "scc_tol": SCC_TOL, "mix_alpha": mix},
+            "set_geometry_s": t_geom, "fp64": {"iteration_s": fp64["iter_s"], "gradients_s": fp64["grad_s"]},
+            "mixed": {"iteration_s": per, "gradients_s": mixed["grad_s"]},
+            "fp64_iteration_vs_mixed_fp32_iteration": t_fp64_iter / per["fp32"],
+            "convergence": counts, "evaluation_model": model_eval}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -728,8 +816,13 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="leave the batched workload out of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--per-iteration", action="store_true",
+                    help="time one iteration of each kind instead of whole evaluations (large configurations)")
+    ap.add_argument("--mix-alpha", type=float, default=0.1, help="Broyden mixing of --per-iteration")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.per_iteration:
+        run_per_iteration(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.config == "batch4096":
         run_batch(args)

@@ -93,7 +93,7 @@ SIGNATURES = {
 
 PHASES = ["h0s_cholesky", "potential_h", "transform", "tridiag", "dc_tridiag", "fermi", "back_transform",
           "density", "mulliken_energy", "broyden", "gradients", "perturbation", "gemm_fp64", "gemm_fp32",
-          "gemm_tc_fp64", "k_sytrd_panel", "k_panel_qr", "k_chase", "k_back_q2"]
+          "gemm_tc_fp64", "k_sytrd_panel", "k_panel_qr", "k_chase", "k_back_q2", "k_sytrd_panel32"]
 
 _lib = None
 

@@ -70,7 +70,7 @@ enum Phase : int {
   kPhH0S = 0, kPhPot, kPhTransform, kPhSytrd, kPhStedc, kPhFermi, kPhBack, kPhDensity, kPhMulliken,
   kPhBroyden, kPhForces, kPhPert, kPhGemm, kPhGemm32, kPhGemmTc,
   // single kernels, timed launch by launch (work = algorithmic bytes or tasks, see the header)
-  kPhKSytrdPanel, kPhKPanelQr, kPhKChase, kPhKBackQ2,
+  kPhKSytrdPanel, kPhKPanelQr, kPhKChase, kPhKBackQ2, kPhKSytrdPanel32,
   kNPhase
 };
 

@@ -491,6 +491,7 @@ struct Q2Args {
   T *Z;
   int ldz;
   int *progress;   // [ngrp * nstrip]: blocks finished per item
+  int *counter;    // next item to take
   int *err;
   int *status;
 };
@@ -513,7 +514,14 @@ __global__ void __launch_bounds__(kQ2Cols / 2) q2_apply_kernel(Q2Args<T> a) {
   __shared__ int ok;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int nitems = a.ngrp * a.nstrip;
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+  __shared__ int s_item;
+  while (true) {
+    // items are taken in index order from a counter: an item waits only on the item nstrip before
+    // it, which a running CTA took earlier
+    if (t == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= nitems) break;
     const int gS = a.ngrp - 1 - item / a.nstrip;
     const int p = item - (item / a.nstrip) * a.nstrip;
     const int cbase = p * kQ2Cols;
@@ -795,8 +803,9 @@ void twostage_back(cudaStream_t s, int n, int k, T *Z, int ldz, const T *V1, int
     const int nstrip = ceil_div(k, kQ2Cols);
     int *ints = reinterpret_cast<int *>(work + L.ints);
     int *err = ints + 8;
+    int *counter = ints + 9;
     int *prog = ints + 16 + n;   // after the chase's progress words
-    cudaMemsetAsync(err, 0, sizeof(int), s);
+    cudaMemsetAsync(err, 0, 2 * sizeof(int), s);
     cudaMemsetAsync(prog, 0, sizeof(int) * (size_t)L.ngrp * nstrip, s);
     static int g_q2 = 0;
     if (g_q2 == 0) {
@@ -804,7 +813,7 @@ void twostage_back(cudaStream_t s, int n, int k, T *Z, int ldz, const T *V1, int
       g_q2 = coop_ctas<T>((const void *)q2_apply_kernel<T>, kQ2Cols / 2, q2_smem_bytes<T>());
     }
     const int G = std::max(1, std::min(g_q2, L.ngrp * nstrip));
-    Q2Args<T> qa{n, k, L.kmax, L.ngrp, nstrip, work + L.V2, work + L.T2, Z, ldz, prog, err, status};
+    Q2Args<T> qa{n, k, L.kmax, L.ngrp, nstrip, work + L.V2, work + L.T2, Z, ldz, prog, counter, err, status};
     void *args[] = {&qa};
     KernelTimer kt(s);
     cudaLaunchCooperativeKernel((const void *)q2_apply_kernel<T>, dim3(G), dim3(kQ2Cols / 2), args, q2_smem_bytes<T>(), s);

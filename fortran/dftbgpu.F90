@@ -180,9 +180,10 @@ module dftbp_extlibs_dftbgpu
       integer(c_int) :: prev
     end function dftbgpu_set_fp64_emulation
 
-    function dftbgpu_set_two_stage(enable) result(prev) bind(C, name="dftbgpu_set_two_stage")
+    !> TwoStage = 0 (one-stage), 1 (two-stage) or 2 (by size, the default); -1 for an invalid mode
+    function dftbgpu_set_two_stage(mode) result(prev) bind(C, name="dftbgpu_set_two_stage")
       import :: c_int
-      integer(c_int), value :: enable
+      integer(c_int), value :: mode
       integer(c_int) :: prev
     end function dftbgpu_set_two_stage
 

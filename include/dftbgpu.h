@@ -210,11 +210,13 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  *   GEMM as tensor-core digit-slice products (mixed form, likewise; FLOPs counted as the FP64
  *   product's 2mnk, the tensor cores execute 36 BF16 products of it). Single kernels, timed launch
  *   by launch (overlapping the phases above; "flops" holds the work in the unit given): 15 one-stage
- *   tridiagonalisation panel kernel (algorithmic bytes: the trailing lower triangle once per
- *   column), 16 two-stage panel QR (bytes: the panel read and written once), 17 bulge chasing
- *   (Householder tasks), 18 two-stage back-transformation of the band stage (FLOPs 2 n^2 k).
- * enable: 1 resets and starts accumulating, 0 stops. read: ms[19], flops[19] (algorithmic FLOPs
- * per phase as counted for the roofline), calls[19]; returns the number of phases written.
+ *   tridiagonalisation panel kernel in FP64 (FLOPs of its symmetric matrix-vector products, 2 m^2
+ *   per column of trailing order m), 16 two-stage panel QR (bytes: the panel read and written
+ *   once), 17 bulge chasing (Householder tasks), 18 two-stage back-transformation of the band stage
+ *   (FLOPs 2 n^2 k), 19 one-stage tridiagonalisation panel kernel in FP32 (bytes: the trailing lower
+ *   triangle once per column).
+ * enable: 1 resets and starts accumulating, 0 stops. read: ms[20], flops[20] (algorithmic FLOPs
+ * per phase as counted for the roofline), calls[20]; returns the number of phases written.
  */
 int dftbgpu_profile_enable(dftbgpu_ctx *ctx, int enable);
 int dftbgpu_profile_read(dftbgpu_ctx *ctx, int nphase, double *ms, double *flops, long long *calls);
