@@ -76,6 +76,8 @@ SIGNATURES = {
     "dftbgpu_set_fp64_emulation": (C.c_int, [C.c_int]),
     "dftbgpu_set_two_stage": (C.c_int, [C.c_int]),
     "dftbgpu_test_twostage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
+    "dftbgpu_set_panel_mode": (C.c_int, [C.c_int]),
+    "dftbgpu_test_onestage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_sgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
                                      C.POINTER(C.c_float), C.c_int, C.c_int]),
@@ -249,6 +251,16 @@ class Context:
                                                   _p(e, C.c_double), _p(q, C.c_double)))
         return d, e[:n - 1], q
 
+    def test_onestage(self, a, fp32=False):
+        """One-stage reduction of the symmetric a: (d, e, q) with a = q tridiag(d, e) q^T."""
+        n = a.shape[0]
+        A = np.asfortranarray(a, dtype=np.float64)
+        d = np.zeros(n); e = np.zeros(max(n - 1, 1))
+        q = np.zeros((n, n), order="F")
+        self.check(self.lib.dftbgpu_test_onestage(self.h, n, _p(A, C.c_double), 1 if fp32 else 0, _p(d, C.c_double),
+                                                  _p(e, C.c_double), _p(q, C.c_double)))
+        return d, e[:n - 1], q
+
     def test_stedc(self, d, e):
         n = len(d)
         dd = np.array(d, dtype=np.float64); ee = np.zeros(max(n - 1, 1)); ee[:n - 1] = e
@@ -387,6 +399,17 @@ def set_fp64_emulation(enable: bool) -> bool:
     """Run the mixed form's FP64 products as exact BF16 digit-slice products on the tensor cores
     (process-wide, on by default); returns the previous setting."""
     return bool(load_library().dftbgpu_set_fp64_emulation(1 if enable else 0))
+
+
+def set_panel_mode(mode) -> int:
+    """Panel kernel of the one-stage tridiagonalisation (process-wide): 0 trailing matrix re-read
+    per column, 1 resident tiles per panel (the default), 2 resident tiles with small limits (tests).
+    Returns the previous mode."""
+    m = int(mode)
+    prev = load_library().dftbgpu_set_panel_mode(m)
+    if prev < 0:
+        raise ValueError(f"panel mode {mode!r}: expected 0, 1 or 2")
+    return prev
 
 
 def set_two_stage(mode) -> int:

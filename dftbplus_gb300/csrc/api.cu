@@ -1000,6 +1000,11 @@ int dftbgpu_set_two_stage(int mode) {
   return g_twostage.exchange(mode);
 }
 
+int dftbgpu_set_panel_mode(int mode) {
+  if (mode < 0 || mode > 2) return -1;
+  return g_panel_mode.exchange(mode);
+}
+
 int dftbgpu_set_fp64_emulation(int enable) {
   const int prev = g_tc_dgemm_mixed ? 1 : 0;
   g_tc_dgemm_mixed = enable != 0;
@@ -1206,6 +1211,7 @@ int dftbgpu_test_tridiag(dftbgpu_ctx *c, int n, const double *a, double *d, doub
   DG_CHECK(c, ensure_orbitals(c, n));
   DG_CUDA(c, cudaMemcpy(c->H, a, sizeof(double) * n * n, cudaMemcpyHostToDevice));
   sytrd_lower(s, n, c->H, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd, c->d_status);
+  DG_CUDA(c, cudaGetLastError());
   DG_CUDA(c, cudaStreamSynchronize(s));
   DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
@@ -1244,7 +1250,43 @@ int dftbgpu_test_twostage(dftbgpu_ctx *c, int n, const double *a, int fp32, doub
     identity_d(s, n, c->Z);
     twostage_back<double>(s, n, n, c->Z, n, c->Vh, n, c->wk_ts, c->d_status);
   }
+  DG_CUDA(c, cudaGetLastError());
   DG_CHECK(c, check_status(c, "two-stage reduction"));
+  DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
+  DG_CUDA(c, cudaMemcpy(q, c->Z, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  c->have_geom = false;
+  c->have_scc = false;
+  c->mixed_ready = false;
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_test_onestage(dftbgpu_ctx *c, int n, const double *a, int fp32, double *d, double *e, double *q) {
+  if (!c || !a || !d || !e || !q || n <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const size_t nn = (size_t)n * n;
+  DG_CHECK(c, ensure_orbitals(c, n));
+  DG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), s));
+  DG_CUDA(c, cudaMemcpyAsync(c->H, a, sizeof(double) * nn, cudaMemcpyHostToDevice, s));
+  if (fp32) {
+    DG_CHECK(c, ensure_mixed_buffers(c, n));
+    convert_d2f(s, nn, c->H, c->A32);
+    sytrd_lower<float>(s, n, c->A32, n, c->d32, c->e32, c->tau32, c->V32, n, c->wk32_sytrd, c->d_status);
+    set_zero_t<float>(s, c->Z32, nn);
+    identity_f(s, n, c->Z32);
+    ormtr_left<float>(s, n, n, c->V32, n, c->tau32, c->Z32, n, c->wk32_ormtr);
+    convert_f2d(s, n, c->d32, c->dd);
+    if (n > 1) convert_f2d(s, n - 1, c->e32, c->ee);
+    convert_f2d(s, nn, c->Z32, c->Z);
+  } else {
+    sytrd_lower(s, n, c->H, n, c->dd, c->ee, c->tau, c->Vh, n, c->wk_sytrd, c->d_status);
+    set_zero(s, c->Z, nn);
+    identity_d(s, n, c->Z);
+    ormtr_left(s, n, n, c->Vh, n, c->tau, c->Z, n, c->wk_ormtr);
+  }
+  DG_CUDA(c, cudaGetLastError());
+  DG_CHECK(c, check_status(c, "one-stage reduction"));
   DG_CUDA(c, cudaMemcpy(d, c->dd, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (n > 1) DG_CUDA(c, cudaMemcpy(e, c->ee, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
   DG_CUDA(c, cudaMemcpy(q, c->Z, sizeof(double) * nn, cudaMemcpyDeviceToHost));

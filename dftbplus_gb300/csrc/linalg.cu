@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(256, 2) sgemm128_kernel(int m, int n, int k, f
 }
 
 std::atomic<bool> g_sgemm128{true};   // FP32 products with many tiles on sgemm128_kernel
+std::atomic<int> g_panel_mode{1};
 
 thread_local GemmProfile g_gemm_prof;
 
@@ -972,16 +973,25 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
     return;
   }
   cudaMemsetAsync(bar, 0, sizeof(GridBar), s);
-  const int G = panel_ctas<T>();
+  PanelResidentPlan plan;
+  const bool resident = g_panel_mode.load() != 0 && panel_resident_plan<T>(n, A, lda, plan);
+  const int G = resident ? plan.ctas : panel_ctas<T>();
   unsigned epoch0 = 0;
   for (int p0 = 0; p0 < n - 1; p0 += PB) {
     int nbp = std::min(PB, n - 1 - p0);
-    PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, dpart, V, d, e, tau, bar, epoch0, status};
-    epoch0 += 3u * (unsigned)nbp;
-    void *args[] = {&pa};
     KernelTimer kt(s);
-    cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
-    count_launch();
+    if (resident) {
+      // two grid barriers per column; wpart holds the per-CTA partials of v^T A22 v
+      panel_resident_launch<T>(s, plan, A, lda, n, p0, nbp, Vp, Wp, P, dots, part, wpart, dpart, V, ldv, d, e, tau,
+                               bar, epoch0, status);
+      epoch0 += 2u * (unsigned)nbp;
+    } else {
+      PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, dpart, V, d, e, tau, bar, epoch0, status};
+      epoch0 += 3u * (unsigned)nbp;
+      void *args[] = {&pa};
+      cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
+      count_launch();
+    }
     // algorithmic work per column j of the panel (m = n - j - 1): FP64 launches count the FLOPs of
     // the symmetric matrix-vector product (2 m^2; the FP64 pipe bounds them), FP32 launches the
     // bytes of the lower triangle of A22 streamed once (m (m + 1) / 2 elements; HBM bounds them)

@@ -111,6 +111,26 @@ template <typename T>
 void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work,
                  int *status = nullptr);
 
+// Panel kernel of sytrd_lower (process-wide): 0 = tiles cut per column and re-read from memory for
+// every column; 1 (default) = trailing tiles fixed per panel, resident in shared memory or streamed
+// by TMA (sytrd_panel.cu) wherever the reduction fits its limits; 2 = as 1 with at most 64 CTAs and
+// 8 tile slots, so that the streaming ring runs at small sizes (tests).
+extern std::atomic<int> g_panel_mode;
+
+struct GridBar;
+// Launch plan of the resident-tile panel kernel for one reduction (A, n, lda fixed).
+struct PanelResidentPlan {
+  bool ok = false, tma = false;
+  int nslot = 0, smem = 0, ctas = 0;
+  alignas(64) unsigned char tmap[128];   // CUtensorMap of A (when tma)
+};
+template <typename T>
+bool panel_resident_plan(int n, T *A, int lda, PanelResidentPlan &p);
+template <typename T>
+void panel_resident_launch(cudaStream_t s, const PanelResidentPlan &p, T *A, int lda, int n, int p0, int nbp, T *Vp,
+                           T *Wp, T *P, T *dots, T *part, T *vpart, T *dpart, T *V, int ldv, T *d, T *e, T *tau,
+                           GridBar *bar, unsigned epoch0, int *status);
+
 // Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: ormtr_work_size<T>(n, k).
 template <typename T>
 size_t ormtr_work_size(int n, int k);

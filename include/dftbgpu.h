@@ -273,6 +273,16 @@ int dftbgpu_set_fp64_emulation(int enable);
  * Process-wide; returns the previous mode, or -1 for an invalid mode (nothing changes).
  */
 int dftbgpu_set_two_stage(int mode);
+/*
+ * Panel kernel of the one-stage tridiagonalisation (no reference counterpart; the reference calls
+ * LAPACK dsytrd/MAGMA through math/eigensolver.F90): mode 1 (the default) keeps the trailing
+ * matrix of each 32-column panel in shared memory (tiles loaded once per panel by TMA, the rest
+ * streamed) with two grid barriers per column, up to 12,288 orbitals in FP32 and 6,144 in FP64;
+ * mode 0 re-reads the trailing matrix from memory for every column (three barriers per column,
+ * any size); mode 2 is mode 1 with at most 64 CTAs and 8 tile slots (for tests of the streaming
+ * path at small sizes). Process-wide; returns the previous mode, or -1 for an invalid mode.
+ */
+int dftbgpu_set_panel_mode(int mode);
 int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                           int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
 /*
@@ -293,6 +303,9 @@ int dftbgpu_test_stedc(dftbgpu_ctx *ctx, int n, double *d, const double *e, doub
 /*   twostage: two-stage reduction of the symmetric a (n x n) in FP32 (fp32 = 1) or FP64 -> d[n],
  *            e[n-1] and q[n*n] = Q1 Q2 (the accumulated transformation, a = q T q^T). */
 int dftbgpu_test_twostage(dftbgpu_ctx *ctx, int n, const double *a, int fp32, double *d, double *e, double *q);
+/*   onestage: one-stage reduction (the panel kernel chosen by dftbgpu_set_panel_mode) in FP32 or
+ *            FP64 -> d[n], e[n-1] and q[n*n] = Q (a = q T q^T). */
+int dftbgpu_test_onestage(dftbgpu_ctx *ctx, int n, const double *a, int fp32, double *d, double *e, double *q);
 
 #ifdef __cplusplus
 }
