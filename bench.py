@@ -257,13 +257,16 @@ def kernel_classes(prof, steps, sm_mhz, dgemm_tflops, sgemm_tflops, workload):
     hbm = hbm_peak()
     bf16 = bf16_peak()
     spec = {
-        "k_sytrd_panel": ("sytrd_panel_kernel<double> (one-stage tridiagonalisation panels, FP64: symmetric "
-                          "matrix-vector products 2 m^2 per column)", "fp64", "TFLOP/s", 1e-12, fp64_cc,
+        "k_sytrd_panel": ("sytrd_panel_resident_kernel<double> (one-stage tridiagonalisation panels, FP64, "
+                          "trailing tiles held per panel: symmetric matrix-vector products 2 m^2 FLOPs per column)",
+                          "fp64", "TFLOP/s", 1e-12, fp64_cc,
                           f"FP64 {N_SM} SMs x 2 FMA x 2 x {f / 1e6:.0f} MHz (cuBLAS DGEMM measured here: "
                           f"{dgemm_tflops:.2f} TFLOP/s)"),
-        "k_sytrd_panel32": ("sytrd_panel_kernel<float> (one-stage tridiagonalisation panels, FP32: trailing lower "
-                            "triangle streamed once per column)", "hbm", "GB/s", 1e-9, hbm,
-                            HBM_PEAK_SOURCE),
+        "k_sytrd_panel32": ("sytrd_panel_resident_kernel<float> (one-stage tridiagonalisation panels, FP32, "
+                            "trailing tiles held per panel: symmetric matrix-vector products 2 m^2 FLOPs per column)",
+                            "fp32", "TFLOP/s", 1e-12, fp32_cc,
+                            f"FP32 CUDA cores {N_SM} SMs x 128 lanes x 2 x {f / 1e6:.0f} MHz (cuBLAS SGEMM measured "
+                            f"here: {sgemm_tflops:.1f} TFLOP/s)"),
         "k_panel_qr": ("panel_qr_kernel (two-stage band reduction, panel QR)", "hbm", "GB/s", 1e-9, hbm,
                        HBM_PEAK_SOURCE),
         "k_back_q2": ("q2_apply_kernel (bulge-chasing reflectors applied to the eigenvectors, FP32)", "fp32",

@@ -111,22 +111,24 @@ static void prof_flops(Ctx *c, int phase, double f) {
 
 // Accumulate elapsed times between consecutive marks (called where the host synchronises anyway).
 static void flush_marks(Ctx *c) {
-  if (!c->prof || c->marks.empty()) return;
-  cudaEventSynchronize(c->marks.back().second);
-  for (size_t i = 0; i + 1 < c->marks.size(); ++i) {
-    int ph = c->marks[i].first;
-    if (ph < 0) continue;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->marks[i].second, c->marks[i + 1].second);
-    c->prof_ms[ph] += ms;
-    c->prof_calls[ph] += 1;
+  if (!c->prof) return;
+  if (!c->marks.empty()) {
+    cudaEventSynchronize(c->marks.back().second);
+    for (size_t i = 0; i + 1 < c->marks.size(); ++i) {
+      int ph = c->marks[i].first;
+      if (ph < 0) continue;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->marks[i].second, c->marks[i + 1].second);
+      c->prof_ms[ph] += ms;
+      c->prof_calls[ph] += 1;
+    }
+    for (size_t i = 0; i + 1 < c->marks.size(); ++i) cudaEventDestroy(c->marks[i].second);
+    std::pair<int, cudaEvent_t> last = c->marks.back();
+    c->marks.clear();
+    if (last.first >= 0) c->marks.push_back(last);
+    else cudaEventDestroy(last.second);
   }
-  for (size_t i = 0; i + 1 < c->marks.size(); ++i) cudaEventDestroy(c->marks[i].second);
-  std::pair<int, cudaEvent_t> last = c->marks.back();
-  c->marks.clear();
-  if (last.first >= 0) c->marks.push_back(last);
-  else cudaEventDestroy(last.second);
-  // GEMM launches
+  // GEMM and kernel-timer launches (also those of the stage test hooks, which set no marks)
   auto &gp = g_gemm_prof;
   for (size_t i = 0; i + 1 < gp.ev.size(); i += 2) {
     cudaEventSynchronize(gp.ev[i + 1]);

@@ -992,13 +992,12 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
       cudaLaunchCooperativeKernel((const void *)sytrd_panel_kernel<T>, dim3(G), dim3(256), args, 0, s);
       count_launch();
     }
-    // algorithmic work per column j of the panel (m = n - j - 1): FP64 launches count the FLOPs of
-    // the symmetric matrix-vector product (2 m^2; the FP64 pipe bounds them), FP32 launches the
-    // bytes of the lower triangle of A22 streamed once (m (m + 1) / 2 elements; HBM bounds them)
+    // algorithmic work per column j of the panel (m = n - j - 1): the FLOPs of the symmetric
+    // matrix-vector product, 2 m^2 (the trailing rank-2k updates are counted with the GEMMs)
     double work = 0.0;
     for (int jj = 0; jj < nbp; ++jj) {
       const double m = (double)(n - (p0 + jj) - 1);
-      work += (sizeof(T) == 8) ? 2.0 * m * m : 0.5 * m * (m + 1.0) * sizeof(T);
+      work += 2.0 * m * m;
     }
     kt.done(sizeof(T) == 8 ? kPhKSytrdPanel : kPhKSytrdPanel32, work);
     int t0 = p0 + nbp;

@@ -133,19 +133,22 @@ __device__ __forceinline__ void tile_of(int idx, int &r, int &c) {
   c = idx - r * (r + 1) / 2;
 }
 
-// Block sum of two values at once (fixed order); every thread gets both totals.
-template <int NT, typename T>
-__device__ void block_sum2(T &x, T &y, T *sh) {
-  x = warp_sum(x);
-  y = warp_sum(y);
+// Block sum of two values at once over the first nw warps (the others hold zeros), fixed order;
+// every thread gets both totals.
+template <typename T>
+__device__ void block_sum2(T &x, T &y, T *sh, int nw) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) {
-    sh[w] = x;
-    sh[32 + w] = y;
+  if (w < nw) {
+    x = warp_sum(x);
+    y = warp_sum(y);
+    if (lane == 0) {
+      sh[w] = x;
+      sh[32 + w] = y;
+    }
   }
   __syncthreads();
   if (threadIdx.x < 32) {
-    T u = (lane < NT / 32) ? sh[lane] : T(0), v = (lane < NT / 32) ? sh[32 + lane] : T(0);
+    T u = (lane < nw) ? sh[lane] : T(0), v = (lane < nw) ? sh[32 + lane] : T(0);
     u = warp_sum(u);
     v = warp_sum(v);
     if (lane == 0) {
@@ -343,6 +346,7 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
           tp = s_scal[1];
           vs = s_scal[2];
         }
+        if (rb + 4 * (t >> 5) >= row1) continue;   // no row of this warp in this pass (warp-uniform)
         T wnew = T(0);
         if (jj > 0) {
           T p = vs * ys;
@@ -383,30 +387,33 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
         }
       }
       if (last) break;
-      // per-CTA partials in one pass: the 4 row groups of a warp, then the 16 warps, fixed order
-      // (W dots at q, V dots at kPb + q, the squared norm at 2 kPb)
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        pdv[i] += __shfl_xor_sync(0xffffffffu, pdv[i], 8);
-        pdv[i] += __shfl_xor_sync(0xffffffffu, pdv[i], 16);
-        pdw[i] += __shfl_xor_sync(0xffffffffu, pdw[i], 8);
-        pdw[i] += __shfl_xor_sync(0xffffffffu, pdw[i], 16);
-      }
-      sig += __shfl_xor_sync(0xffffffffu, sig, 8);
-      sig += __shfl_xor_sync(0xffffffffu, sig, 16);
+      // per-CTA partials in one pass: the 4 row groups of a warp, then the warps that had rows
+      // (w < nused), fixed order (W dots at q, V dots at kPb + q, the squared norm at 2 kPb)
       constexpr int kW = 2 * kPb + 1;
-      if (lane < 8) {
+      const int nused = min(kThreads / 32, max(0, (row1 - row0 + 3) / 4));
+      if ((t >> 5) < nused) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          pdv[i] += __shfl_xor_sync(0xffffffffu, pdv[i], 8);
+          pdv[i] += __shfl_xor_sync(0xffffffffu, pdv[i], 16);
+          pdw[i] += __shfl_xor_sync(0xffffffffu, pdw[i], 8);
+          pdw[i] += __shfl_xor_sync(0xffffffffu, pdw[i], 16);
+        }
+        sig += __shfl_xor_sync(0xffffffffu, sig, 8);
+        sig += __shfl_xor_sync(0xffffffffu, sig, 16);
+      }
+      if (lane < 8 && (t >> 5) < nused) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           red[(t >> 5) * kW + lane + 8 * i] = pdw[i];
           red[(t >> 5) * kW + kPb + lane + 8 * i] = pdv[i];
         }
       }
-      if (lane == 0) red[(t >> 5) * kW + 2 * kPb] = sig;
+      if (lane == 0 && (t >> 5) < nused) red[(t >> 5) * kW + 2 * kPb] = sig;
       __syncthreads();
       if (t < kW) {
         T sp = T(0);
-        for (int w = 0; w < kThreads / 32; ++w) sp += red[w * kW + t];
+        for (int w = 0; w < nused; ++w) sp += red[w * kW + t];
         if (t < 2 * kPb)
           a.dpart[(size_t)b * 2 * kPb + t] = sp;
         else
@@ -441,7 +448,7 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
         const int kk = t + kThreads * k;
         if (kk < vlen) vall[kk] = raw[k];
       }
-      block_sum2<kThreads>(ssum, dp, sh);
+      block_sum2(ssum, dp, sh, (G + 31) / 32);   // only threads t < G hold partials
       if (t == 0) {
         // dlarfg: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta, v = x / (alpha - beta)
         T beta, tv, scale;

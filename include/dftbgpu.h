@@ -213,8 +213,7 @@ long long dftbgpu_kernel_launches(const dftbgpu_ctx *ctx);
  *   tridiagonalisation panel kernel in FP64 (FLOPs of its symmetric matrix-vector products, 2 m^2
  *   per column of trailing order m), 16 two-stage panel QR (bytes: the panel read and written
  *   once), 17 bulge chasing (Householder tasks), 18 two-stage back-transformation of the band stage
- *   (FLOPs 2 n^2 k), 19 one-stage tridiagonalisation panel kernel in FP32 (bytes: the trailing lower
- *   triangle once per column).
+ *   (FLOPs 2 n^2 k), 19 one-stage tridiagonalisation panel kernel in FP32 (FLOPs as 15).
  * enable: 1 resets and starts accumulating, 0 stops. read: ms[20], flops[20] (algorithmic FLOPs
  * per phase as counted for the roofline), calls[20]; returns the number of phases written.
  */
