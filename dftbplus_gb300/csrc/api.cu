@@ -395,15 +395,17 @@ static int eigensolve(Ctx *c, int n, double *Hm, PickK pick_k, bool reduced = fa
   return DFTBGPU_OK;
 }
 
-// The reduced non-SCC Hamiltonian A0 = L^-1 H0 L^-T (lower), once per geometry, formed by the first
-// SCC call so that the mixed form can run its two products on the tensor cores (g_tc_dgemm set by
-// the caller); the plain form forms it in FP64 arithmetic.
+// L^-1 and the reduced non-SCC Hamiltonian A0 = L^-1 H0 L^-T (lower), once per geometry, formed by
+// the first SCC call so that the mixed form can run their products on the tensor cores (g_tc_dgemm
+// set by the caller); the plain form forms them in FP64 arithmetic. (The Cholesky factor itself is
+// computed by set_geometry, which reports an overlap that is not positive definite.)
 static int ensure_a0(Ctx *c) {
   if (c->have_a0) return DFTBGPU_OK;
   cudaStream_t s = c->stream;
   const int n = c->norb;
   mark(c, kPhH0S);
-  prof_flops(c, kPhH0S, 2.0 / 3.0 * (double)n * n * n);
+  prof_flops(c, kPhH0S, (double)n * n * n);
+  trtri_lower(s, n, c->Lc, n, c->Linv, n, c->T, (size_t)n * n);
   dgemm(s, 'N', 'T', n, n, n, 1.0, c->H0, n, c->Linv, n, 0.0, c->T, n, kBUpper);
   dgemm(s, 'N', 'N', n, n, n, 1.0, c->Linv, n, c->T, n, 0.0, c->A0, n, kALower | kCLower);
   c->have_a0 = true;
@@ -649,11 +651,10 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   prof_flops(c, kPhH0S, (double)norb * norb * norb / 3.0);
   build_h0_s(s, m, g, c->d_pi, c->d_pj, np, c->H0, c->S);
   repulsive_energy(s, m, g, c->d_eatom, c->d_scal);
-  // Cholesky of S, L^-1, and the reduced non-SCC Hamiltonian A0 = L^-1 H0 L^-T (lower)
+  // Cholesky of S (L^-1 and A0 = L^-1 H0 L^-T follow in the first SCC call: ensure_a0)
   DG_CUDA(c, cudaMemcpyAsync(c->Lc, c->S, sizeof(double) * (size_t)norb * norb, cudaMemcpyDeviceToDevice, s));
   potrf_lower(s, norb, c->Lc, norb, c->d_status);
   DG_CHECK(c, check_status(c, "Cholesky of S"));
-  trtri_lower(s, norb, c->Lc, norb, c->Linv, norb, c->T, (size_t)norb * norb);
   mark(c, -1);
   DG_CUDA(c, cudaGetLastError());
   DG_CUDA(c, cudaStreamSynchronize(s));

@@ -95,8 +95,8 @@ struct KernelTimer {
 // In-place lower Cholesky A = L L^T (strict upper set to 0). status_dev[0] != 0 on failure.
 void potrf_lower(cudaStream_t s, int n, double *A, int lda, int *status_dev);
 
-// X = L^{-1} for lower-triangular L (X lower, strict upper zero). work: >= 64*n doubles (more is
-// used as split-K space).
+// X = L^{-1} for lower-triangular L (X lower, strict upper zero), recursively on halves. work: >=
+// n*n/4 doubles (more is used as split-K space).
 void trtri_lower(cudaStream_t s, int n, const double *L, int ldl, double *X, int ldx, double *work,
                  size_t work_elems);
 
