@@ -77,6 +77,7 @@ SIGNATURES = {
     "dftbgpu_set_two_stage": (C.c_int, [C.c_int]),
     "dftbgpu_test_twostage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_set_panel_mode": (C.c_int, [C.c_int]),
+    "dftbgpu_set_digit_gemm_kernel": (C.c_int, [C.c_int]),
     "dftbgpu_test_onestage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_sgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
                                      C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
@@ -399,6 +400,16 @@ def set_fp64_emulation(enable: bool) -> bool:
     """Run the mixed form's FP64 products as exact BF16 digit-slice products on the tensor cores
     (process-wide, on by default); returns the previous setting."""
     return bool(load_library().dftbgpu_set_fp64_emulation(1 if enable else 0))
+
+
+def set_digit_gemm_kernel(mode) -> int:
+    """Kernel of the FP64-class tensor-core products (process-wide): 0 single-stage (the default),
+    1 pipelined with TMA loads. Returns the previous mode."""
+    m = int(mode)
+    prev = load_library().dftbgpu_set_digit_gemm_kernel(m)
+    if prev < 0:
+        raise ValueError(f"digit GEMM kernel {mode!r}: expected 0 or 1")
+    return prev
 
 
 def set_panel_mode(mode) -> int:

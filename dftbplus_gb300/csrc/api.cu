@@ -1003,6 +1003,11 @@ int dftbgpu_set_two_stage(int mode) {
   return g_twostage.exchange(mode);
 }
 
+int dftbgpu_set_digit_gemm_kernel(int mode) {
+  if (mode < 0 || mode > 1) return -1;
+  return g_dg_kernel.exchange(mode);
+}
+
 int dftbgpu_set_panel_mode(int mode) {
   if (mode < 0 || mode > 2) return -1;
   return g_panel_mode.exchange(mode);

@@ -48,6 +48,9 @@ int tc_dgemm_error();
 // g_tc_dgemm_mixed allows it).
 extern thread_local bool g_tc_dgemm;        // per calling thread
 extern std::atomic<bool> g_tc_dgemm_mixed;  // process-wide switch
+// Kernel of tc_dgemm (process-wide): 0 (default) the single-stage kernel (one 64-wide K block per
+// round trip of copies, MMAs and readback); 1 pipelined, TMA-fed, windowed TMEM readback.
+extern std::atomic<int> g_dg_kernel;
 
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,

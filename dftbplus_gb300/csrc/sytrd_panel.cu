@@ -29,6 +29,7 @@
 #include "gridsync.cuh"
 #include "linalg.cuh"
 #include "tcgen05.cuh"
+#include "tma.cuh"
 
 namespace dg {
 
@@ -558,18 +559,6 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
   if (t == 0 && a.status != nullptr && *(volatile int *)&a.bar->err != 0) atomicMax(a.status, (int)kDevIterCap);
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 f = [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }();
-  return f;
-}
-
 }  // namespace
 
 template <typename T>
@@ -578,12 +567,12 @@ bool panel_resident_plan(int n, T *A, int lda, PanelResidentPlan &p) {
   const int vlen = (n + kTile - 1) / kTile * kTile;
   if (n < 2 || vlen > kThreads * kVPer<T>) return false;
   const bool aligned = ((uintptr_t)A % 16 == 0) && (((size_t)lda * sizeof(T)) % 16 == 0);
-  if (aligned && encode_fn() != nullptr) {
+  if (aligned && tensor_map_encoder() != nullptr) {
     CUtensorMap *m = reinterpret_cast<CUtensorMap *>(p.tmap);
     const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
     const cuuint64_t strides[1] = {(cuuint64_t)lda * sizeof(T)};
     const cuuint32_t box[2] = {kTile, kTile}, es[2] = {1, 1};
-    const CUresult r = encode_fn()(m, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+    const CUresult r = tensor_map_encoder()(m, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                                    (void *)A, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);

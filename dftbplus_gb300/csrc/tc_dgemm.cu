@@ -42,6 +42,7 @@
 #include "linalg.cuh"
 #include "scratch.cuh"
 #include "tcgen05.cuh"
+#include "tma.cuh"
 
 namespace dg {
 
@@ -53,6 +54,7 @@ constexpr int DG_BTILE = DG_BN * DG_BK * 2;               // 8 KB: one digit sla
 constexpr int DG_STAGE = DG_S * (DG_ATILE + DG_BTILE);    // 192 KB
 constexpr int DG_SMEM = DG_STAGE + 1024 + 64;             // alignment slack + barrier, TMEM slot, flag
 constexpr uint32_t DG_TMEM_COLS = 512;                    // 8 groups x 64 columns
+constexpr int DG_GROUP_M = 8;                             // row tiles per group of the tile order
 
 // Scale exponent E of a row from the bit pattern of its largest magnitude: max < 2^E.
 __device__ __forceinline__ int dg_row_exp(unsigned long long maxbits) {
@@ -182,7 +184,14 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
                                                               long long *P, int kb_split) {
   extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int i0 = blockIdx.x * DG_BM, j0 = blockIdx.y * DG_BN;
+  // output tiles in groups of DG_GROUP_M row tiles (all column tiles of a group before the next), so
+  // that the CTAs resident at one time share the K-slices of a few A panels in L2
+  const int ntm = gridDim.x, ntn = gridDim.y;
+  const int bid = blockIdx.x + ntm * blockIdx.y;
+  const int first_m = bid / (DG_GROUP_M * ntn) * DG_GROUP_M;
+  const int gm = min(ntm - first_m, DG_GROUP_M);
+  const int local = bid % (DG_GROUP_M * ntn);
+  const int i0 = (first_m + local % gm) * DG_BM, j0 = (local / gm) * DG_BN;
   if ((flags & kCLower) && j0 > i0 + DG_BM - 1) return;   // tile above the diagonal, before any TMEM use
   // K-blocks that can hold non-zero products (triangular operands), as in the FP64 GEMM
   int kbeg = 0, kend = Kp;
@@ -335,6 +344,223 @@ __global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_kernel(int m, int n, in
   if (t == 0 && failed) atomicExch(err, 1);
 }
 
+// ------------------------------------------------------------------------------ pipelined kernel
+// The same products and exactness argument as dg_gemm_kernel, organised as a pipeline:
+//   * one TMA load per operand and K-sub-block of 32 brings all eight digit slabs of the A (128 x 32)
+//     and B (64 x 32) tiles into shared memory with the 64-byte swizzle (96 KB per stage, two
+//     stages), from 3D tensor maps over the packed slabs (K, row, slab);
+//   * thread 0 issues the 72 MMAs of a sub-block (36 products x 2 K-steps of 16) and commits them to
+//     the stage's "empty" barrier; the load two sub-blocks ahead waits only for that barrier, so the
+//     copies run under the MMAs;
+//   * the eight group sums stay in TMEM for a window of 8 sub-blocks (K = 256): a group sum is an
+//     integer of magnitude <= 8 x 256 x 2^12 = 2^23, still exact in FP32 whatever the order of the
+//     additions; at the end of a window all eight warps read the sums back (an exact float -> int32
+//     conversion; 2^7 G_g + G_{g+1} < 2^31) into the int64 accumulators, while the next window's
+//     first copies are in flight;
+//   * output tiles are visited in groups of 8 row tiles (all column tiles of a group before the next
+//     group), so the CTAs resident at one time share the K-slices of 8 A panels and of the column
+//     panels they walk, which stay in L2.
+constexpr int DG2_SK = 32;                                  // K per sub-block (one stage)
+constexpr int DG2_WIN = 8;                                  // sub-blocks per TMEM readback window
+constexpr int DG2_ASLAB = DG_BM * DG2_SK * 2;               // 8 KB: one digit slab of the A tile
+constexpr int DG2_BSLAB = DG_BN * DG2_SK * 2;               // 4 KB
+constexpr int DG2_STAGE = DG_S * (DG2_ASLAB + DG2_BSLAB);   // 96 KB
+constexpr int DG2_SMEM = 2 * DG2_STAGE + 1024 + 128;        // alignment slack + barriers, TMEM slot, flag
+
+// Shared-memory matrix descriptor: K-major operand tile with the 64-byte swizzle (64-byte rows of 32
+// BF16), 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t dg2_sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);   // start address
+  d |= (uint64_t)1 << 16;                     // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;            // stride byte offset between 8-row groups
+  d |= (uint64_t)1 << 46;                     // descriptor version
+  d |= (uint64_t)4 << 61;                     // 64-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void dg2_arrive_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void dg2_tma3(uint32_t dst, const void *map, int x, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          dst),
+      "l"(map), "r"(x), "r"(y), "r"(0), "r"(mbar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(DG_THREADS, 1) dg_gemm_tma_kernel(
+    const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int m, int n, int Kp,
+    int Mp, int Np, const unsigned long long *rmaxA, const unsigned long long *rmaxB, int R, double alpha,
+    double beta, double *C, int ldc, int flags, int *err, long long *P, int kb_split) {
+  extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  // grouped tile order
+  const int ntm = gridDim.x, ntn = gridDim.y;
+  const int bid = blockIdx.x + ntm * blockIdx.y;
+  const int first_m = bid / (DG_GROUP_M * ntn) * DG_GROUP_M;
+  const int gm = min(ntm - first_m, DG_GROUP_M);
+  const int local = bid % (DG_GROUP_M * ntn);
+  const int i0 = (first_m + local % gm) * DG_BM, j0 = (local / gm) * DG_BN;
+  if ((flags & kCLower) && j0 > i0 + DG_BM - 1) return;   // tile above the diagonal, before any TMEM use
+  int kbeg = 0, kend = Kp;
+  if (flags & kALower) kend = min(kend, i0 + DG_BM);
+  if (flags & kAUpper) kbeg = max(kbeg, i0);
+  if (flags & kBLower) kbeg = max(kbeg, j0);
+  if (flags & kBUpper) kend = min(kend, j0 + DG_BN);
+  int kb0 = kbeg / DG_BK, kb1 = (kend + DG_BK - 1) / DG_BK;
+  if (P != nullptr) {
+    kb0 += blockIdx.z * kb_split;
+    kb1 = min(kb1, kb0 + kb_split);
+  }
+  const int nsub = kb1 > kb0 ? 2 * (kb1 - kb0) : 0;
+  const int kfirst = kb0 * DG_BK;
+
+  const uint32_t raw = smem_u32(dg_smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  unsigned char *sm = dg_smem_raw + (base - raw);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 2 * DG2_STAGE);   // full[2], empty[2], tfull
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 2 * DG2_STAGE + 64);
+  volatile int *sfail = reinterpret_cast<volatile int *>(sm + 2 * DG2_STAGE + 72);
+  auto full = [&](int st) { return smem_u32(&bars[st]); };
+  auto empty = [&](int st) { return smem_u32(&bars[2 + st]); };
+  const uint32_t tfull = smem_u32(&bars[4]);
+  if (t == 0) {
+    for (int b = 0; b < 5; ++b) mbar_init(smem_u32(&bars[b]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sfail = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(DG_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  auto load = [&](int i) {   // thread 0: sub-block i into stage i & 1
+    const int st = i & 1;
+    const uint32_t sa = base + st * DG2_STAGE, sb = sa + DG_S * DG2_ASLAB;
+    dg2_arrive_tx(full(st), DG2_STAGE);
+    dg2_tma3(sa, &mapA, kfirst + i * DG2_SK, i0, full(st));
+    dg2_tma3(sb, &mapB, kfirst + i * DG2_SK, j0, full(st));
+  };
+  int next_load = 0, consumed = 0;   // thread 0: sub-blocks loaded / whose copies were waited for
+  if (t == 0) {
+    for (; next_load < 2 && next_load < nsub; ++next_load) load(next_load);
+  }
+  const int quad = warp & 3, half = warp >> 2;
+  long long acc[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) acc[c] = 0;
+  for (int w0 = 0, win = 0; w0 < nsub; w0 += DG2_WIN, ++win) {
+    const int w1 = min(nsub, w0 + DG2_WIN);
+    if (t == 0) {
+      for (int i = w0; i < w1 && !*sfail; ++i) {
+        if (!mbar_wait(full(i & 1), (uint32_t)((i >> 1) & 1))) {
+          *sfail = 1;
+          break;
+        }
+        consumed = i + 1;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = base + (i & 1) * DG2_STAGE, sb = sa + DG_S * DG2_ASLAB;
+        const uint64_t da0 = dg2_sdesc(sa), db0 = dg2_sdesc(sb);
+#pragma unroll
+        for (int g = 0; g < DG_S; ++g)
+#pragma unroll
+          for (int s = 0; s <= g; ++s)
+#pragma unroll
+            for (int kk = 0; kk < DG2_SK / 16; ++kk)
+              tc_mma(tmem + (uint32_t)(g * DG_BN), da0 + (uint64_t)((s * DG2_ASLAB + kk * 32) >> 4),
+                     db0 + (uint64_t)(((g - s) * DG2_BSLAB + kk * 32) >> 4), dg_idesc(),
+                     (i > w0 || s > 0 || kk > 0) ? 1u : 0u);
+        tc_commit(empty(i & 1));
+        if (next_load == i + 1 && next_load < nsub) {
+          // the stage of sub-block i + 1 held sub-block i - 1: free once its MMAs completed
+          if (i >= 1 && !mbar_wait(empty((i - 1) & 1), (uint32_t)(((i - 1) >> 1) & 1))) {
+            *sfail = 1;
+            break;
+          }
+          load(next_load++);
+        }
+      }
+      tc_commit(tfull);   // arrives once every MMA issued so far has completed
+    }
+    if (!mbar_wait(tfull, (uint32_t)(win & 1))) *sfail = 1;
+    __syncthreads();
+    if (*sfail) break;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // the window's last sub-block is done: its stage takes the sub-block after next
+    if (t == 0 && next_load == w1 + 1 && next_load < nsub) load(next_load++);
+    const uint32_t tlane = tmem + ((uint32_t)(quad * 32) << 16);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+      for (int g = 0; g < DG_S; g += 2) {
+        uint32_t va[16], vb[16];
+        tc_ld16(tlane + (uint32_t)(g * DG_BN + half * 32 + h * 16), va);
+        tc_ld16(tlane + (uint32_t)((g + 1) * DG_BN + half * 32 + h * 16), vb);
+        tc_wait_ld2x16(va, vb);
+        const int sh = 7 * (DG_S - 2 - g) - R;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const unsigned ga = (unsigned)__float2int_rn(__uint_as_float(va[c]));
+          const unsigned gb = (unsigned)__float2int_rn(__uint_as_float(vb[c]));
+          const int p = (int)((ga << 7) + gb);   // |2^7 G_g + G_{g+1}| < 2^31
+          long long &a = acc[h * 16 + c];
+          if (sh >= 0) a += (long long)p << sh;
+          else a += (long long)((p + (1 << (-sh - 1))) >> (-sh));
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();   // TMEM free for the next window
+  }
+  const bool failed = *sfail != 0;
+  if (failed && t == 0) {
+    // copies still in flight: wait (bounded) for each before the shared memory goes away
+    for (int i = consumed; i < next_load; ++i) mbar_wait(full(i & 1), (uint32_t)((i >> 1) & 1));
+  }
+  if (!failed && P != nullptr) {
+    long long *Pz = P + (size_t)blockIdx.z * Mp * Np;
+    const int row = i0 + quad * 32 + lane;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) Pz[row + (size_t)(j0 + half * 32 + c) * Mp] = acc[c];
+  } else if (!failed) {
+    const int row = i0 + quad * 32 + lane;
+    if (row < m) {
+      const unsigned long long ma = rmaxA[row];
+      const int ea = dg_row_exp(ma) - 61 + R;
+      const bool bad_a = (ma >> 52) >= 2047ull;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int col = j0 + half * 32 + c;
+        if (col < n && (!(flags & kCLower) || row >= col)) {
+          const unsigned long long mb = rmaxB[col];
+          double x = ldexp((double)acc[c], ea + dg_row_exp(mb));
+          if (bad_a || (mb >> 52) >= 2047ull) x = __longlong_as_double(0x7FF8000000000000ll);
+          x *= alpha;
+          double *cp = C + row + (size_t)col * ldc;
+          if (beta != 0.0) x = fma(beta, *cp, x);
+          *cp = x;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DG_TMEM_COLS) : "memory");
+  }
+  if (t == 0 && failed) atomicExch(err, 1);
+}
+
 // C = alpha 2^(EA_i + EB_j - 61 + R) sum_z P[z] + beta C over the elements a split-K product computed
 // (integer sums: the result does not depend on the split).
 __global__ void dg_splitk_reduce(int m, int n, int Mp, int Np, int splits, const long long *__restrict__ P,
@@ -359,6 +585,7 @@ __global__ void dg_splitk_reduce(int m, int n, int Mp, int Np, int splits, const
 // ------------------------------------------------------------------------------ host side
 thread_local bool g_tc_dgemm = false;   // gemm<double> routes here while set (calling thread only)
 std::atomic<bool> g_tc_dgemm_mixed{true};   // dftbgpu_set_fp64_emulation
+std::atomic<int> g_dg_kernel{0};            // 0: single-stage kernel, 1: pipelined TMA kernel
 constexpr int kDgSMs = 148;   // CTAs in flight (one per SM; GB300 has 152, a few may be taken)
 // scratch of this thread on the current device: digit slabs, row maxima, split-K partials
 static thread_local ThreadScratch t_dg;
@@ -372,8 +599,23 @@ static int dg_ensure(DeviceScratch &d, size_t ws_elems, size_t rmax_elems) {
   if (rc == 0 && !d.err) {
     rc = scratch_err(d);
     if (rc == 0) rc = (int)cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM);
+    if (rc == 0)
+      rc = (int)cudaFuncSetAttribute(dg_gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DG2_SMEM);
   }
   return rc;
+}
+
+// 3D tensor map over packed digit slabs (K innermost, then rows, then the eight slabs) with a box of
+// 32 K x box_rows rows x 8 slabs and the 64-byte swizzle; false if the driver cannot encode it.
+static bool dg_slab_map(CUtensorMap *map, const __nv_bfloat16 *slabs, int rows, int Kp, int box_rows) {
+  auto enc = tensor_map_encoder();
+  if (enc == nullptr) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)DG_S};
+  const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+  const cuuint32_t box[3] = {(cuuint32_t)DG2_SK, (cuuint32_t)box_rows, (cuuint32_t)DG_S}, es[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)slabs, dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // K-splits for a product with few output tiles: enough CTAs to fill the GPU, at least four K-blocks
@@ -430,8 +672,13 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
     Pp = static_cast<long long *>(ds.buf[kDgPart].p);
     kb_split = ceil_div(Kp / DG_BK, splits);
   }
-  dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG_SMEM, s>>>(
-      m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
+  CUtensorMap mapA, mapB;
+  if (g_dg_kernel.load() == 1 && dg_slab_map(&mapA, PA, Mp, Kp, DG_BM) && dg_slab_map(&mapB, PB, Np, Kp, DG_BN))
+    dg_gemm_tma_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG2_SMEM, s>>>(
+        mapA, mapB, m, n, Kp, Mp, Np, rA, rB, R, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
+  else
+    dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG_SMEM, s>>>(
+        m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
   count_launch(3);
   if (Pp) {
     const int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);

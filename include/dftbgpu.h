@@ -263,6 +263,15 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k
  */
 int dftbgpu_set_fp64_emulation(int enable);
 /*
+ * Kernel of those FP64-class products (no reference counterpart): 0 (the default) runs the
+ * single-stage kernel (one 64-wide K block, 128-byte-swizzled, per round of copies, products and
+ * readback); 1 feeds the tensor cores through a two-stage pipeline of TMA loads (K-sub-blocks of 32,
+ * 64-byte swizzle) and reads the group sums back from tensor memory once per 256-wide K window (it
+ * measures slower on GB300). Both give the same FP64-class error bound. Process-wide; returns the
+ * previous mode, or -1 for an invalid mode.
+ */
+int dftbgpu_set_digit_gemm_kernel(int mode);
+/*
  * Two-stage reduction for the FP32 eigensolves of the mixed form (no reference counterpart; the
  * reference reaches two-stage reductions through ELPA, elecsolvers/elecsolvertypes.F90:27, and
  * MAGMA's dsygvd_m, math/eigensolver.F90:1143-1245): the matrix is reduced to a band of width 32 with

@@ -9,6 +9,15 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=[0, 1], ids=["single-stage", "pipelined"])
+def dg_kernel(request, gpu_lib):
+    """Both kernels of the digit-slice product: the pipelined TMA kernel and the single-stage one."""
+    from dftbplus_gb300 import binding
+    prev = binding.set_digit_gemm_kernel(request.param)
+    yield request.param
+    binding.set_digit_gemm_kernel(prev)
+
+
 def _ref(ta, tb, A, B):
     a = A.T if ta == "T" else A
     b = B.T if tb == "T" else B
@@ -75,7 +84,7 @@ def _dref(ta, tb, A, B):
     (64, 64, 2000, "T", "N"),      # one tile, long K: split over 8 CTAs along K
     (64, 512, 1500, "T", "N"),     # few tiles: split along K
 ])
-def test_tc_dgemm_products(gpu_lib, m, n, k, ta, tb):
+def test_tc_dgemm_products(gpu_lib, dg_kernel, m, n, k, ta, tb):
     from dftbplus_gb300 import binding
     rng = np.random.default_rng(m * 5 + n + k)
     A = rng.standard_normal((k, m) if ta == "T" else (m, k))
@@ -87,7 +96,7 @@ def test_tc_dgemm_products(gpu_lib, m, n, k, ta, tb):
     ctx.close()
 
 
-def test_tc_dgemm_scales_zeros_and_flags(gpu_lib):
+def test_tc_dgemm_scales_zeros_and_flags(gpu_lib, dg_kernel):
     """Rows and columns over 60 orders of magnitude, zero rows, triangular hints, lower-only output
     and beta accumulation; the untouched upper triangle keeps its bits."""
     from dftbplus_gb300 import binding
@@ -111,7 +120,7 @@ def test_tc_dgemm_scales_zeros_and_flags(gpu_lib):
     ctx.close()
 
 
-def test_tc_dgemm_split_lower_beta(gpu_lib):
+def test_tc_dgemm_split_lower_beta(gpu_lib, dg_kernel):
     """Split-K with a lower-only output and beta accumulation (int64 partials summed exactly): the
     same product split and unsplit agree bit for bit."""
     from dftbplus_gb300 import binding
@@ -136,9 +145,10 @@ def test_tc_dgemm_split_lower_beta(gpu_lib):
     ctx.close()
 
 
-def test_tc_dgemm_largest_digit_sums(gpu_lib):
-    """Every digit 63 but the last: block group sums near the 2^21 bound must stay exact in the
-    tensor-memory FP32 accumulators (K = 1,024, so 16 K blocks are read back)."""
+def test_tc_dgemm_largest_digit_sums(gpu_lib, dg_kernel):
+    """Every digit 63 but the last: group sums near their bound must stay exact in the tensor-memory
+    FP32 accumulators (K = 1,024: 16 blocks of 64 read back, sums near 2^21, in the single-stage
+    kernel; 4 windows of 256, sums near 2^23, in the pipelined one)."""
     from dftbplus_gb300 import binding
     Y = 63 * sum(128 ** j for j in range(1, 8))
     x = Y * 2.0 ** -54
