@@ -18,6 +18,7 @@ module dftbp_extlibs_dftbgpu
   public :: dftbgpu_set_model, dftbgpu_set_geometry, dftbgpu_scc, dftbgpu_scc_history
   public :: dftbgpu_gradients, dftbgpu_n_orbitals, dftbgpu_get_orbital_populations
   public :: dftbgpu_set_tensor_cores, dftbgpu_set_fp64_emulation, dftbgpu_set_two_stage
+  public :: dftbgpu_set_panel_mode, dftbgpu_set_digit_gemm_kernel
   public :: dftbgpuErrorMessage
   public :: DFTBGPU_OK, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_CUDA, DFTBGPU_ERR_NOT_POSDEF, &
       & DFTBGPU_ERR_SCC_NOT_CONVERGED, DFTBGPU_ERR_FERMI, DFTBGPU_ERR_ITER_CAP, DFTBGPU_ERR_STATE, &
@@ -186,6 +187,21 @@ module dftbp_extlibs_dftbgpu
       integer(c_int), value :: mode
       integer(c_int) :: prev
     end function dftbgpu_set_two_stage
+
+    !> PanelKernel = 1 (trailing tiles on chip per panel, the default), 0 (re-read per column) or 2
+    !> (on-chip kernel with small limits, tests); -1 for an invalid mode
+    function dftbgpu_set_panel_mode(mode) result(prev) bind(C, name="dftbgpu_set_panel_mode")
+      import :: c_int
+      integer(c_int), value :: mode
+      integer(c_int) :: prev
+    end function dftbgpu_set_panel_mode
+
+    !> Fp64EmulationKernel = 0 (single-stage, the default) or 1 (TMA-pipelined); -1 for an invalid mode
+    function dftbgpu_set_digit_gemm_kernel(mode) result(prev) bind(C, name="dftbgpu_set_digit_gemm_kernel")
+      import :: c_int
+      integer(c_int), value :: mode
+      integer(c_int) :: prev
+    end function dftbgpu_set_digit_gemm_kernel
 
   end interface
 
