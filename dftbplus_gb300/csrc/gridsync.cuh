@@ -70,4 +70,30 @@ __device__ __forceinline__ void grid_sync(GridBar *b, unsigned nb, unsigned &epo
   __syncthreads();
 }
 
+// The same barrier for a launch whose grid size may differ from that of the earlier launches on the
+// same counter: the counter stood at `base` when the launch started, so barrier e of the launch
+// completes when it reaches base + (e + 1) * nb. Thread 0 runs before_arrive() after the entry
+// __syncthreads and before its arrival (the release orders what it writes before the arrival).
+template <class F>
+__device__ __forceinline__ void grid_sync_base(GridBar *b, unsigned nb, unsigned base, unsigned &e, F before_arrive) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    before_arrive();
+    volatile int *verr = &b->err;
+    if (*verr == 0) {
+      asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&b->count), "r"(1u) : "memory");
+      const unsigned target = base + (e + 1u) * nb;
+      unsigned it = 0;
+      while ((int)(grid_load_acquire(&b->count) - target) < 0) {
+        if (++it > kBarrierSpinLimit) {
+          atomicExch(&b->err, 1);
+          break;
+        }
+      }
+    }
+  }
+  ++e;
+  __syncthreads();
+}
+
 }  // namespace dg

@@ -994,10 +994,11 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
     int nbp = std::min(PB, n - 1 - p0);
     KernelTimer kt(s);
     if (resident) {
-      // two grid barriers per column; wpart holds the per-CTA partials of v^T A22 v
-      panel_resident_launch<T>(s, plan, A, lda, n, p0, nbp, Vp, Wp, P, dots, part, wpart, dpart, V, ldv, d, e, tau,
-                               bar, epoch0, status);
-      epoch0 += 2u * (unsigned)nbp;
+      // two grid barriers per column; wpart holds the per-CTA partials of v^T A22 v; epoch0 counts
+      // barrier arrivals
+      panel_resident_launch<T>(s, plan, plan.ctas, A, lda, n, p0, nbp, Vp, Wp, P, dots, part, wpart, dpart, V, ldv,
+                               d, e, tau, bar, epoch0, status);
+      epoch0 += 2u * (unsigned)nbp * (unsigned)plan.ctas;
     } else {
       PanelArgs<T> pa{A, lda, n, p0, nbp, ldv, Vp, Wp, y, P, dots, part, wpart, dpart, V, d, e, tau, bar, epoch0, status};
       epoch0 += 3u * (unsigned)nbp;
@@ -1028,19 +1029,27 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
 // ------------------------------------------------------------------------------------- ormtr
 constexpr int OB = 64;
 
-// T (nb x nb, upper) of the compact WY form: H_p..H_{p+nb-1} = I - V T V^T, from G = V^T V.
+// T (nb x nb, upper, nb <= OB) of the compact WY form: H_p..H_{p+nb-1} = I - V T V^T, from G = V^T V
+// (leading dimension ldg), written to Tf (leading dimension ldt). The upper triangle of G is staged in
+// shared memory first, so the serial recurrence T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i) reads only
+// shared memory.
 template <typename T>
-__global__ void larft_kernel(int nb, const T *G, const T *tau, T *Tf) {
-  __shared__ T t[OB][OB + 1];
+__global__ void larft_kernel(int nb, const T *G, int ldg, const T *tau, T *Tf, int ldt) {
+  extern __shared__ __align__(16) unsigned char larft_smem[];
+  T(*t)[OB + 1] = reinterpret_cast<T(*)[OB + 1]>(larft_smem);
+  T(*g)[OB + 1] = t + OB;
   const int tid = threadIdx.x;
-  for (int k = tid; k < OB * OB; k += blockDim.x) t[k % OB][k / OB] = T(0);
+  for (int k = tid; k < OB * OB; k += blockDim.x) {
+    const int r = k % OB, c = k / OB;
+    t[r][c] = T(0);
+    g[r][c] = (r <= c && c < nb) ? G[r + (size_t)c * ldg] : T(0);
+  }
   __syncthreads();
   for (int i = 0; i < nb; ++i) {
-    // t(0:i, i) = -tau_i * T(0:i, 0:i) * G(0:i, i)
-    T ti = tau[i];
+    const T ti = tau[i];
     T v = T(0);
     if (tid < i) {
-      for (int q = tid; q < i; ++q) v = fma(t[tid][q], G[q + (size_t)i * nb], v);
+      for (int q = tid; q < i; ++q) v = fma(t[tid][q], g[q][i], v);
       v *= -ti;
     }
     __syncthreads();
@@ -1048,42 +1057,68 @@ __global__ void larft_kernel(int nb, const T *G, const T *tau, T *Tf) {
     if (tid == 0) t[i][i] = ti;
     __syncthreads();
   }
-  for (int k = tid; k < nb * nb; k += blockDim.x) Tf[k] = t[k % nb][k / nb];
+  for (int k = tid; k < nb * nb; k += blockDim.x) Tf[k % nb + (size_t)(k / nb) * ldt] = t[k % nb][k / nb];
+}
+
+template <typename T>
+static void larft_launch(cudaStream_t s, int nb, const T *G, int ldg, const T *tau, T *Tf, int ldt) {
+  constexpr int kSmem = 2 * OB * (OB + 1) * (int)sizeof(T);
+  static const bool attr = [] {
+    cudaFuncSetAttribute(larft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    return true;
+  }();
+  (void)attr;
+  larft_kernel<T><<<1, OB, kSmem, s>>>(nb, G, ldg, tau, Tf, ldt);
+  count_launch();
 }
 
 template <typename T>
 void larft(cudaStream_t s, int nb, const T *G, const T *tau, T *Tf) {
-  larft_kernel<T><<<1, OB, 0, s>>>(nb, G, tau, Tf);
-  count_launch();
+  larft_launch<T>(s, nb, G, nb, tau, Tf, nb);
 }
 template void larft<float>(cudaStream_t, int, const float *, const float *, float *);
 template void larft<double>(cudaStream_t, int, const double *, const double *, double *);
 
+// Z is updated by blocks of OB2 reflectors: two larft blocks of OB merged into one compact WY form,
+// T = [[T1, -T1 (V1^T V2) T2], [0, T2]] (H1 H2 = I - [V1 V2] T [V1 V2]^T), so that the two large
+// products of a block have 128 rows and a K of 128.
+constexpr int OB2 = 2 * OB;
+
 template <typename T>
 size_t ormtr_work_size(int n, int k) {
-  // G, T, M, M2 + split-K partials (up to 8 slices of the larger of OB x k and OB x OB)
-  return 2 * (size_t)OB * OB + 2 * (size_t)OB * std::max(k, 1) + 8 * (size_t)OB * std::max(k, OB);
+  // G, T (OB2 x OB2), X (OB x OB), M, M2 (OB2 x k) + split-K partials (8 slices of OB2 x max(k, OB2))
+  return 2 * (size_t)OB2 * OB2 + (size_t)OB * OB + 2 * (size_t)OB2 * std::max(k, 1) +
+         8 * (size_t)OB2 * std::max(k, OB2);
 }
 
 template <typename T>
 void ormtr_left(cudaStream_t s, int n, int k, const T *V, int ldv, const T *tau, T *Z, int ldz, T *work) {
   if (n <= 1 || k <= 0) return;
   T *G = work;
-  T *Tf = G + OB * OB;
-  T *M = Tf + OB * OB;
-  T *M2 = M + (size_t)OB * k;
-  T *SP = M2 + (size_t)OB * k;
-  const size_t sp_elems = 8 * (size_t)OB * std::max(k, OB);
+  T *Tf = G + OB2 * OB2;
+  T *X = Tf + OB2 * OB2;
+  T *M = X + OB * OB;
+  T *M2 = M + (size_t)OB2 * k;
+  T *SP = M2 + (size_t)OB2 * k;
+  const size_t sp_elems = 8 * (size_t)OB2 * std::max(k, OB2);
   int nref = n - 1;  // reflectors j = 0 .. n-2
-  int last = ((nref - 1) / OB) * OB;
-  for (int p0 = last; p0 >= 0; p0 -= OB) {
-    int nb = std::min(OB, nref - p0);
+  int last = ((nref - 1) / OB2) * OB2;
+  for (int p0 = last; p0 >= 0; p0 -= OB2) {
+    const int nb = std::min(OB2, nref - p0);
+    const int n1 = std::min(nb, OB), n2 = nb - n1;
     int r0 = p0 + 1;          // first nonzero row of the block's vectors
     int mr = n - r0;
     const T *Vb = V + r0 + (size_t)p0 * ldv;
     gemm<T>(s, 'T', 'N', nb, nb, mr, T(1), Vb, ldv, Vb, ldv, T(0), G, nb, 0, SP, sp_elems);
-    larft_kernel<T><<<1, OB, 0, s>>>(nb, G, tau + p0, Tf);
-    count_launch();
+    set_zero_t<T>(s, Tf, (size_t)nb * nb);
+    larft_launch<T>(s, n1, G, nb, tau + p0, Tf, nb);
+    if (n2 > 0) {
+      larft_launch<T>(s, n2, G + n1 + (size_t)n1 * nb, nb, tau + p0 + n1, Tf + n1 + (size_t)n1 * nb, nb);
+      // T12 = -T1 G12 T2 with G12 = V1^T V2: X = G12 T2, then T12 = -T1 X (T1, T2 upper)
+      gemm<T>(s, 'N', 'N', n1, n2, n2, T(1), G + (size_t)n1 * nb, nb, Tf + n1 + (size_t)n1 * nb, nb, T(0), X, n1,
+              kBUpper);
+      gemm<T>(s, 'N', 'N', n1, n2, n1, T(-1), Tf, nb, X, n1, T(0), Tf + (size_t)n1 * nb, nb, kAUpper);
+    }
     gemm<T>(s, 'T', 'N', nb, k, mr, T(1), Vb, ldv, Z + r0, ldz, T(0), M, nb, 0, SP, sp_elems);
     gemm<T>(s, 'N', 'N', nb, k, nb, T(1), Tf, nb, M, nb, T(0), M2, nb, kAUpper);
     gemm<T>(s, 'N', 'N', mr, k, nb, T(-1), Vb, ldv, M2, nb, T(1), Z + r0, ldz);

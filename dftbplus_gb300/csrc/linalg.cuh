@@ -129,10 +129,12 @@ struct PanelResidentPlan {
 };
 template <typename T>
 bool panel_resident_plan(int n, T *A, int lda, PanelResidentPlan &p);
+// One panel (columns p0 .. p0 + nbp - 1) on `ctas` CTAs (at most p.ctas); the grid barrier counter
+// stands at `base` when it starts and gains 2 nbp ctas arrivals.
 template <typename T>
-void panel_resident_launch(cudaStream_t s, const PanelResidentPlan &p, T *A, int lda, int n, int p0, int nbp, T *Vp,
-                           T *Wp, T *P, T *dots, T *part, T *vpart, T *dpart, T *V, int ldv, T *d, T *e, T *tau,
-                           GridBar *bar, unsigned epoch0, int *status);
+void panel_resident_launch(cudaStream_t s, const PanelResidentPlan &p, int ctas, T *A, int lda, int n, int p0, int nbp,
+                           T *Vp, T *Wp, T *P, T *dots, T *part, T *vpart, T *dpart, T *V, int ldv, T *d, T *e,
+                           T *tau, GridBar *bar, unsigned base, int *status);
 
 // Z (n x k) <- Q Z with Q = H_0 ... H_{n-2} from sytrd_lower. work: ormtr_work_size<T>(n, k).
 template <typename T>

@@ -56,7 +56,7 @@ struct Args {
   T *V, *d, *e, *tau;
   int ldv;
   GridBar *bar;
-  unsigned epoch0;
+  unsigned base;   // the barrier counter when the launch starts
   int *status;
 };
 
@@ -134,35 +134,6 @@ __device__ __forceinline__ void tile_of(int idx, int &r, int &c) {
   c = idx - r * (r + 1) / 2;
 }
 
-// Block sum of two values at once over the first nw warps (the others hold zeros), fixed order;
-// every thread gets both totals.
-template <typename T>
-__device__ void block_sum2(T &x, T &y, T *sh, int nw) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (w < nw) {
-    x = warp_sum(x);
-    y = warp_sum(y);
-    if (lane == 0) {
-      sh[w] = x;
-      sh[32 + w] = y;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    T u = (lane < nw) ? sh[lane] : T(0), v = (lane < nw) ? sh[32 + lane] : T(0);
-    u = warp_sum(u);
-    v = warp_sum(v);
-    if (lane == 0) {
-      sh[0] = u;
-      sh[32] = v;
-    }
-  }
-  __syncthreads();
-  x = sh[0];
-  y = sh[32];
-  __syncthreads();
-}
-
 // Eight per-lane values summed over the 16 lanes of a half warp (lanes differing in bits 0..3):
 // lane l returns the total of value (l >> 1) & 7 (8 shuffles).
 template <typename T>
@@ -221,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
   T *vall = slots + (size_t)a.nslot * kTile * kTile;
   T *red = vall + vlen;
   const unsigned nb = (unsigned)G;
-  unsigned epoch = a.epoch0;
+  unsigned epoch = 0;   // barriers of this launch
   constexpr uint32_t kTileBytes = kTile * kTile * sizeof(T);
 
   // This CTA's tiles b, b + G, ... (k = 0 .. K-1) are shared among four groups of 128 threads
@@ -421,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
           a.part[b] = sp;
       }
     }
-    grid_sync(a.bar, nb, epoch);
+    grid_sync_base(a.bar, nb, a.base, epoch, [] {});
     // ------------------------------------------------------------------------------------- B
     {
       T ssum = (t < G) ? __ldcg(a.part + t) : T(0);
@@ -449,8 +420,23 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
         const int kk = t + kThreads * k;
         if (kk < vlen) vall[kk] = raw[k];
       }
-      block_sum2(ssum, dp, sh, (G + 31) / 32);   // only threads t < G hold partials
+      // the two sums over the CTAs' partials: the warps that hold them (threads t < G), then thread 0
+      if ((t >> 5) < (G + 31) / 32) {
+        ssum = warp_sum(ssum);
+        dp = warp_sum(dp);
+        if (lane == 0) {
+          sh[t >> 5] = ssum;
+          sh[32 + (t >> 5)] = dp;
+        }
+      }
+      __syncthreads();
       if (t == 0) {
+        ssum = T(0);
+        dp = T(0);
+        for (int w = 0; w < (G + 31) / 32; ++w) {
+          ssum += sh[w];
+          dp += sh[32 + w];
+        }
         // dlarfg: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta, v = x / (alpha - beta)
         T beta, tv, scale;
         if (ssum == T(0)) {
@@ -551,10 +537,15 @@ __global__ void __launch_bounds__(kThreads, 1) sytrd_panel_resident_kernel(const
           vacc = fma(vall[r0 + tg], sr, vacc);
         }
       }
-      vacc = block_sum<kThreads>(vacc, sh);
-      if (t == 0) a.vpart[b] = vacc;
+      vacc = warp_sum(vacc);
+      if (lane == 0) sh[t >> 5] = vacc;
     }
-    grid_sync(a.bar, nb, epoch);
+    // the CTA's partial of v^T A22 v, summed over the warps by thread 0 at the barrier's entry
+    grid_sync_base(a.bar, nb, a.base, epoch, [&] {
+      T v = T(0);
+      for (int w = 0; w < kThreads / 32; ++w) v += sh[w];
+      a.vpart[b] = v;
+    });
   }
   if (t == 0 && a.status != nullptr && *(volatile int *)&a.bar->err != 0) atomicMax(a.status, (int)kDevIterCap);
 }
@@ -609,28 +600,28 @@ bool panel_resident_plan(int n, T *A, int lda, PanelResidentPlan &p) {
 }
 
 template <typename T>
-void panel_resident_launch(cudaStream_t s, const PanelResidentPlan &p, T *A, int lda, int n, int p0, int nbp, T *Vp,
-                           T *Wp, T *P, T *dots, T *part, T *vpart, T *dpart, T *V, int ldv, T *d, T *e, T *tau,
-                           GridBar *bar, unsigned epoch0, int *status) {
-  Args<T> a{A, lda, n, p0, nbp, p.nslot, Vp, Wp, P, dots, part, vpart, dpart, V, d, e, tau, ldv, bar, epoch0, status};
+void panel_resident_launch(cudaStream_t s, const PanelResidentPlan &p, int ctas, T *A, int lda, int n, int p0, int nbp,
+                           T *Vp, T *Wp, T *P, T *dots, T *part, T *vpart, T *dpart, T *V, int ldv, T *d, T *e,
+                           T *tau, GridBar *bar, unsigned base, int *status) {
+  Args<T> a{A, lda, n, p0, nbp, p.nslot, Vp, Wp, P, dots, part, vpart, dpart, V, d, e, tau, ldv, bar, base, status};
   CUtensorMap map;
   std::memcpy(&map, p.tmap, sizeof(map));
   void *args[] = {&map, &a};
   if (p.tma)
-    cudaLaunchCooperativeKernel((const void *)sytrd_panel_resident_kernel<T, true>, dim3(p.ctas), dim3(kThreads), args,
+    cudaLaunchCooperativeKernel((const void *)sytrd_panel_resident_kernel<T, true>, dim3(ctas), dim3(kThreads), args,
                                 (size_t)p.smem, s);
   else
-    cudaLaunchCooperativeKernel((const void *)sytrd_panel_resident_kernel<T, false>, dim3(p.ctas), dim3(kThreads), args,
+    cudaLaunchCooperativeKernel((const void *)sytrd_panel_resident_kernel<T, false>, dim3(ctas), dim3(kThreads), args,
                                 (size_t)p.smem, s);
   count_launch();
 }
 
 template bool panel_resident_plan<float>(int, float *, int, PanelResidentPlan &);
 template bool panel_resident_plan<double>(int, double *, int, PanelResidentPlan &);
-template void panel_resident_launch<float>(cudaStream_t, const PanelResidentPlan &, float *, int, int, int, int, float *,
-                                           float *, float *, float *, float *, float *, float *, float *, int, float *,
-                                           float *, float *, GridBar *, unsigned, int *);
-template void panel_resident_launch<double>(cudaStream_t, const PanelResidentPlan &, double *, int, int, int, int,
+template void panel_resident_launch<float>(cudaStream_t, const PanelResidentPlan &, int, float *, int, int, int, int,
+                                           float *, float *, float *, float *, float *, float *, float *, float *, int,
+                                           float *, float *, float *, GridBar *, unsigned, int *);
+template void panel_resident_launch<double>(cudaStream_t, const PanelResidentPlan &, int, double *, int, int, int, int,
                                             double *, double *, double *, double *, double *, double *, double *,
                                             double *, int, double *, double *, double *, GridBar *, unsigned, int *);
 
