@@ -947,8 +947,8 @@ __global__ void copy_last_diag_kernel(int n, const T *A, int lda, T *d) {
 template <typename T>
 size_t sytrd_work_size(int n) {
   size_t nt = (size_t)ceil_div(n, ST);
-  // Vp, Wp, y, P, dots, part, wpart, dpart, barrier (16 elements)
-  return 2 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 2 * (size_t)kMaxPanelCtas +
+  // Vp, Wp, a copy of Vp, y, P, dots, part, wpart, dpart, barrier (16 elements)
+  return 3 * (size_t)n * PB + (size_t)n + nt * nt * ST + 2 * PB + 2 * (size_t)kMaxPanelCtas +
          2 * (size_t)PB * kMaxPanelCtas + 16;
 }
 
@@ -971,7 +971,8 @@ template <typename T>
 void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V, int ldv, T *work, int *status) {
   T *Vp = work;
   T *Wp = Vp + (size_t)n * PB;
-  T *y = Wp + (size_t)n * PB;
+  T *Vp2 = Wp + (size_t)n * PB;   // [Vp | Wp] and [Wp | Vp2] are n x 2 PB matrices
+  T *y = Vp2 + (size_t)n * PB;
   T *P = y + n;
   size_t T0 = (size_t)ceil_div(n, ST);
   T *dots = P + T0 * T0 * ST;
@@ -1018,8 +1019,15 @@ void sytrd_lower(cudaStream_t s, int n, T *A, int lda, T *d, T *e, T *tau, T *V,
     int m2 = n - t0;
     if (m2 > 0) {
       T *At = A + t0 + (size_t)t0 * lda;
-      gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Vp + t0, n, Wp + t0, n, T(1), At, lda, kCLower);
-      gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Wp + t0, n, Vp + t0, n, T(1), At, lda, kCLower);
+      if (nbp == PB) {
+        // one rank-2 PB update: A22 -= [V W] [W V]^T, with the copy of V placed after W
+        cudaMemcpy2DAsync(Vp2 + t0, (size_t)n * sizeof(T), Vp + t0, (size_t)n * sizeof(T), (size_t)m2 * sizeof(T),
+                          PB, cudaMemcpyDeviceToDevice, s);
+        gemm<T>(s, 'N', 'T', m2, m2, 2 * PB, T(-1), Vp + t0, n, Wp + t0, n, T(1), At, lda, kCLower);
+      } else {
+        gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Vp + t0, n, Wp + t0, n, T(1), At, lda, kCLower);
+        gemm<T>(s, 'N', 'T', m2, m2, nbp, T(-1), Wp + t0, n, Vp + t0, n, T(1), At, lda, kCLower);
+      }
     }
   }
   copy_last_diag_kernel<T><<<1, 1, 0, s>>>(n, A, lda, d);
