@@ -87,6 +87,10 @@ SIGNATURES = {
     "dftbgpu_test_gemm_tc": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
                                        C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
                                        C.POINTER(C.c_float), C.c_int, C.c_int]),
+    "dftbgpu_test_sgemm_digits": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
+                                            C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.c_int, C.c_float,
+                                            C.POINTER(C.c_float), C.c_int, C.c_int]),
+    "dftbgpu_set_fp32_emulation": (C.c_int, [C.c_int]),
     "dftbgpu_test_tridiag": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_stedc": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
@@ -323,6 +327,20 @@ class Context:
                                                  _p(Cm, C_float), m, flags))
         return Cm
 
+    def test_sgemm_digits(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):
+        """C = alpha op(A) op(B) + beta C as exact BF16 digit-slice products on the tensor cores
+        (FP32-class; float32, column-major)."""
+        A = np.asfortranarray(A, dtype=np.float32)
+        B = np.asfortranarray(B, dtype=np.float32)
+        m = A.shape[1] if ta == "T" else A.shape[0]
+        k = A.shape[0] if ta == "T" else A.shape[1]
+        n = B.shape[0] if tb == "T" else B.shape[1]
+        Cm = np.zeros((m, n), dtype=np.float32, order="F") if C is None else np.array(C, dtype=np.float32, order="F")
+        self.check(self.lib.dftbgpu_test_sgemm_digits(self.h, ta.encode(), tb.encode(), m, n, k, alpha,
+                                                      _p(A, C_float), A.shape[0], _p(B, C_float), B.shape[0], beta,
+                                                      _p(Cm, C_float), m, flags))
+        return Cm
+
     def test_sgemm(self, ta, tb, A, B, C=None, alpha=1.0, beta=0.0, flags=0):
         """C = alpha op(A) op(B) + beta C with the library's FP32 FMA GEMM (float32, column-major)."""
         A = np.asfortranarray(A, dtype=np.float32)
@@ -394,6 +412,12 @@ class Context:
 def set_tensor_cores(enable: bool) -> bool:
     """Route the large FP32 products of the mixed form to the tcgen05 tensor cores (process-wide)."""
     return bool(load_library().dftbgpu_set_tensor_cores(1 if enable else 0))
+
+
+def set_fp32_emulation(enable: bool) -> bool:
+    """Run the FP32 products of the mixed form's FP32 eigensolves as exact BF16 digit-slice products on
+    the tensor cores (process-wide, on by default); returns the previous setting."""
+    return bool(load_library().dftbgpu_set_fp32_emulation(1 if enable else 0))
 
 
 def set_fp64_emulation(enable: bool) -> bool:

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdftbgpu.so")
-SOURCES = ["api.cu", "linalg.cu", "stedc.cu", "dftb_kernels.cu", "batch.cu", "adjoint.cu", "tc_gemm.cu", "tc_dgemm.cu", "twostage.cu", "sytrd_panel.cu"]
+SOURCES = ["api.cu", "linalg.cu", "stedc.cu", "dftb_kernels.cu", "batch.cu", "adjoint.cu", "tc_gemm.cu", "tc_dgemm.cu", "twostage.cu", "sytrd_panel.cu", "tc_fgemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-diag-suppress", "550"]

@@ -726,7 +726,10 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
   // gemm<double> goes to the tensor-core digit-slice product only inside the mixed form's FP64
   // iterations; the guard switches it off again on every return path
   struct RouteGuard {
-    ~RouteGuard() { g_tc_dgemm = false; }
+    ~RouteGuard() {
+      g_tc_dgemm = false;
+      g_tc_fgemm = false;
+    }
   } route_guard;
   c->hist_e.clear(); c->hist_err.clear(); c->hist_ms.clear(); c->hist_prec.clear();
   int mix_calls = 0;
@@ -746,6 +749,7 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     if (mixed && it == o->max_iter) form = kFormFull;   // the last allowed iteration is FP64
     const int it_form = form;
     g_tc_dgemm = mixed && g_tc_dgemm_mixed && form == kFormFull;
+    g_tc_fgemm = mixed && g_tc_fgemm_mixed;   // FP32 products of the FP32 eigensolves and the reference
     mark(c, kPhPot);
     potential(s, m, g, c->d_qin, c->d_q0, c->d_V);
     int k = 0;
@@ -853,9 +857,10 @@ int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init,
     DG_CUDA(c, cudaMemcpyAsync(h_scal, c->d_scal, sizeof(h_scal), cudaMemcpyDeviceToHost, s));
     DG_CUDA(c, cudaStreamSynchronize(s));
     DG_CUDA(c, cudaGetLastError());
-    if (mixed && (tc_dgemm_error() || tc_gemm_error()))
+    if (mixed && (tc_dgemm_error() || tc_gemm_error() || tc_fgemm_error()))
       return set_error(c, DFTBGPU_ERR_ITER_CAP, "tensor-core GEMM: a bounded wait timed out");
     g_tc_dgemm = false;
+    g_tc_fgemm = false;
     flush_marks(c);
     c->hist_e.push_back(h_scal[kSEnonScc] + h_scal[kSEscc]);
     c->hist_err.push_back(h_scal[kSErr]);
@@ -1065,6 +1070,36 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, 
   if (rc != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tc_gemm: %s", cudaGetErrorString((cudaError_t)rc));
   if (tc_gemm_error()) return set_error(c, DFTBGPU_ERR_ITER_CAP, "tc_gemm: a bounded wait timed out");
   return DFTBGPU_OK;
+}
+
+int dftbgpu_test_sgemm_digits(dftbgpu_ctx *c, char ta, char tb, int m, int n, int k, float alpha, const float *a,
+                              int lda, const float *b, int ldb, float beta, float *cm, int ldc, int flags) {
+  if (!c || !a || !b || !cm || m <= 0 || n <= 0 || k <= 0) return DFTBGPU_ERR_ARGS;
+  cudaSetDevice(c->device);
+  const size_t na = (size_t)lda * ((ta == 'N') ? k : m), nb = (size_t)ldb * ((tb == 'N') ? n : k),
+               nc = (size_t)ldc * n;
+  float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  DG_CUDA(c, cudaMalloc((void **)&dA, na * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dB, nb * sizeof(float)));
+  DG_CUDA(c, cudaMalloc((void **)&dC, nc * sizeof(float)));
+  DG_CUDA(c, cudaMemcpy(dA, a, na * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dB, b, nb * sizeof(float), cudaMemcpyHostToDevice));
+  DG_CUDA(c, cudaMemcpy(dC, cm, nc * sizeof(float), cudaMemcpyHostToDevice));
+  const int rc = tc_fgemm(c->stream, ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, flags);
+  DG_CUDA(c, cudaStreamSynchronize(c->stream));
+  DG_CUDA(c, cudaMemcpy(cm, dC, nc * sizeof(float), cudaMemcpyDeviceToHost));
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  if (rc != 0) return set_error(c, DFTBGPU_ERR_CUDA, "tc_fgemm: %s", cudaGetErrorString((cudaError_t)rc));
+  if (tc_fgemm_error()) return set_error(c, DFTBGPU_ERR_ITER_CAP, "tc_fgemm: a bounded wait timed out");
+  return DFTBGPU_OK;
+}
+
+int dftbgpu_set_fp32_emulation(int enable) {
+  const int prev = g_tc_fgemm_mixed ? 1 : 0;
+  g_tc_fgemm_mixed = enable != 0;
+  return prev;
 }
 
 int dftbgpu_profile_enable(dftbgpu_ctx *c, int enable) {

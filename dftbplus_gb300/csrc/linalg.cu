@@ -343,8 +343,15 @@ void gemm(cudaStream_t s, char ta, char tb, int m, int n, int k, T alpha, const 
     }
   }
   if constexpr (std::is_same<T, float>::value) {
+    if (g_tc_fgemm && m >= 512 && n >= 512 && k >= 512 && cap == cudaStreamCaptureStatusNone) {
+      // a scratch allocation that fails leaves the product to the FP32 FMA kernels below
+      if (tc_fgemm(s, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags) == 0) {
+        done = true;
+        P = nullptr;
+      }
+    }
     const long long tiles128 = (long long)ceil_div(m, 128) * ceil_div(n, 128);
-    if (g_sgemm128 && tiles128 >= 2 * 152) {
+    if (!done && g_sgemm128 && tiles128 >= 2 * 152) {
       const dim3 g128(ceil_div(m, 128), ceil_div(n, 128));
       if (!TA && !TB)
         sgemm128_kernel<false, false><<<g128, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, flags);

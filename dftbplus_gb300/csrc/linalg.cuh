@@ -52,6 +52,16 @@ extern std::atomic<bool> g_tc_dgemm_mixed;  // process-wide switch
 // round trip of copies, MMAs and readback); 1 pipelined, TMA-fed, windowed TMEM readback.
 extern std::atomic<int> g_dg_kernel;
 
+// FP32-class product on the tensor cores (tc_fgemm.cu): exact BF16 digit-slice products (three
+// signed 8-bit digits per element, six products, integer accumulation), same arguments and flags as
+// gemm. Returns a cudaError_t value. While g_tc_fgemm is set, gemm<float> sends products with m, n, k
+// >= 512 there (the mixed form sets it around its FP32 eigensolves when g_tc_fgemm_mixed allows it).
+int tc_fgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha, const float *A, int lda,
+             const float *B, int ldb, float beta, float *C, int ldc, int flags);
+int tc_fgemm_error();
+extern thread_local bool g_tc_fgemm;        // per calling thread
+extern std::atomic<bool> g_tc_fgemm_mixed;  // process-wide switch
+
 void dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha, const double *A,
            int lda, const double *B, int ldb, double beta, double *C, int ldc, int flags = 0,
            double *work = nullptr, size_t work_elems = 0);

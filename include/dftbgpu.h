@@ -263,6 +263,21 @@ int dftbgpu_test_gemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k
  */
 int dftbgpu_set_fp64_emulation(int enable);
 /*
+ * FP32-class products of the mixed form on the tensor cores (no reference counterpart): when enabled
+ * (the default), the FP32 GEMMs of its FP32 eigensolves (reduced transform, divide-and-conquer
+ * merges, back-transformation, density matrix) and of the FP64 iterations' FP32 reference products
+ * with m, n, k >= 512 run as exact products of BF16 digit slices on tcgen05: three signed 8-bit digits
+ * per element at a power-of-two scale per row (column), six products, group sums exact in FP32 per
+ * 64-wide K block, int64 accumulation. The error of an element is below about
+ * K max|A_ik| max|B_kj| 2^-23 (FP32-class), with no rounding bias over long K. The plain FP64 form
+ * never uses it. Process-wide; returns the previous setting. dftbgpu_test_sgemm_digits runs one such
+ * product on host arrays (column-major, flags as the library's triangular GEMM hints).
+ */
+int dftbgpu_set_fp32_emulation(int enable);
+int dftbgpu_test_sgemm_digits(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, float alpha,
+                              const float *a, int lda, const float *b, int ldb, float beta, float *c, int ldc,
+                              int flags);
+/*
  * Kernel of those FP64-class products (no reference counterpart): 0 (the default) runs the
  * single-stage kernel (one 64-wide K block, 128-byte-swizzled, per round of copies, products and
  * readback); 1 feeds the tensor cores through a two-stage pipeline of TMA loads (K-sub-blocks of 32,

@@ -197,3 +197,95 @@ def test_sgemm_large_tiles_flags_beta(gpu_lib):
     assert np.all(np.abs(C - ref)[low] <= 1e-6 * mag[low] + 1e-6)
     assert np.array_equal(C[~low], C0[~low])
     ctx.close()
+
+
+# ------------------------------------------------------------------ FP32-class digit-slice products
+def _fref(ta, tb, A, B):
+    a = (A.T if ta == "T" else A).astype(np.float64)
+    b = (B.T if tb == "T" else B).astype(np.float64)
+    k = a.shape[1]
+    # operand rounding (2^-25 of the row / column maxima), the dropped digit groups (2^-24) and the
+    # final rounding to FP32
+    scale = k * np.abs(a).max(1)[:, None] * np.abs(b).max(0)[None, :]
+    ref = a @ b
+    return ref, scale * 2.0 ** -22 + np.abs(ref) * 2.0 ** -23
+
+
+@pytest.mark.parametrize("m,n,k,ta,tb", [
+    (128, 64, 64, "N", "N"),       # one tile, one K block
+    (256, 192, 200, "N", "N"),     # several tiles and K blocks (both stages), ragged K
+    (300, 200, 130, "N", "T"),     # ragged edges, padding
+    (384, 257, 640, "T", "N"),
+    (129, 511, 77, "T", "T"),
+    (64, 512, 1500, "T", "N"),     # few tiles: split along K
+    (1000, 900, 3000, "N", "T"),
+])
+def test_fp32_digit_products(gpu_lib, m, n, k, ta, tb):
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(m * 7 + n + k)
+    A = rng.standard_normal((k, m) if ta == "T" else (m, k)).astype(np.float32)
+    B = rng.standard_normal((n, k) if tb == "T" else (k, n)).astype(np.float32)
+    ctx = binding.Context(0)
+    C = ctx.test_sgemm_digits(ta, tb, A, B)
+    ref, tol = _fref(ta, tb, A, B)
+    assert np.all(np.abs(C - ref) <= tol), np.max(np.abs(C - ref) / tol)
+    ctx.close()
+
+
+def test_fp32_digit_scales_zeros_and_flags(gpu_lib):
+    """Rows and columns over 20 orders of magnitude, a zero row, triangular hints, lower-only output
+    and beta accumulation; the untouched upper triangle keeps its bits."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(12)
+    n = 320
+    L = (np.tril(rng.standard_normal((n, n))) * 10.0 ** rng.uniform(-10, 10, (n, 1))).astype(np.float32)
+    L[17] = 0.0
+    junk = np.triu(rng.standard_normal((n, n)), 1).astype(np.float32)   # must be ignored (kALower)
+    X = (rng.standard_normal((n, n)) * 10.0 ** rng.uniform(-3, 3, (1, n))).astype(np.float32)
+    C0 = rng.standard_normal((n, n)).astype(np.float32)
+    ctx = binding.Context(0)
+    kALower, kCLower = 1, 16
+    C = ctx.test_sgemm_digits("N", "N", L + junk, X, C=C0, alpha=0.5, beta=1.0, flags=kALower | kCLower)
+    ref, tol = _fref("N", "N", L, X)
+    ref = 0.5 * ref + C0
+    tol = 0.5 * tol + 2.0 ** -22 * np.abs(C0) + np.abs(ref) * 2.0 ** -23
+    low = np.tril(np.ones((n, n), dtype=bool))
+    assert np.all(np.abs(C - ref)[low] <= tol[low]), np.max((np.abs(C - ref) / tol)[low])
+    assert np.array_equal(C[~low], C0[~low])
+    assert np.array_equal(C[17, :18], C0[17, :18])          # zero row: alpha * 0 + beta * C0
+    ctx.close()
+
+
+def test_fp32_digit_split_lower_beta(gpu_lib):
+    """Split-K with a lower-only output and beta accumulation (int64 partials summed exactly)."""
+    from dftbplus_gb300 import binding
+    rng = np.random.default_rng(22)
+    m, k = 256, 1200                 # 4 x 4 tiles (lower half computed), 19 K blocks: split 4 ways
+    A = rng.standard_normal((m, k)).astype(np.float32)
+    B = rng.standard_normal((k, m)).astype(np.float32)
+    C0 = rng.standard_normal((m, m)).astype(np.float32)
+    ctx = binding.Context(0)
+    kCLower = 16
+    C = ctx.test_sgemm_digits("N", "N", A, B, C=C0, alpha=-1.0, beta=1.0, flags=kCLower)
+    ref, tol = _fref("N", "N", A, B)
+    ref = C0 - ref
+    tol = tol + 2.0 ** -22 * np.abs(C0)
+    low = np.tril(np.ones((m, m), dtype=bool))
+    assert np.all(np.abs(C - ref)[low] <= tol[low])
+    assert np.array_equal(C[~low], C0[~low])
+    ctx.close()
+
+
+def test_fp32_digit_largest_group_sums(gpu_lib):
+    """x = 1 - 2^-24 has the digits (256, 0, -1): the leading group sum of a 64-wide K block is 2^22,
+    next to its bound, and must stay exact in the tensor-memory FP32 accumulators (K = 1,024)."""
+    from dftbplus_gb300 import binding
+    x = np.float32(1.0) - np.float32(2.0 ** -24)
+    k = 1024
+    A = np.full((128, k), x, dtype=np.float32)
+    B = np.full((k, 64), -x, dtype=np.float32)
+    ctx = binding.Context(0)
+    C = ctx.test_sgemm_digits("N", "N", A, B)
+    exact = -k * float(x) * float(x)
+    assert np.all(np.abs(C.astype(np.float64) - exact) <= abs(exact) * 2.0 ** -23)
+    ctx.close()
