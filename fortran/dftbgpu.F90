@@ -18,7 +18,7 @@ module dftbp_extlibs_dftbgpu
   public :: dftbgpu_set_model, dftbgpu_set_geometry, dftbgpu_scc, dftbgpu_scc_history
   public :: dftbgpu_gradients, dftbgpu_n_orbitals, dftbgpu_get_orbital_populations
   public :: dftbgpu_set_tensor_cores, dftbgpu_set_fp64_emulation, dftbgpu_set_two_stage
-  public :: dftbgpu_set_panel_mode, dftbgpu_set_digit_gemm_kernel
+  public :: dftbgpu_set_panel_mode, dftbgpu_set_digit_gemm_kernel, dftbgpu_set_fp32_emulation
   public :: dftbgpuErrorMessage
   public :: DFTBGPU_OK, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_CUDA, DFTBGPU_ERR_NOT_POSDEF, &
       & DFTBGPU_ERR_SCC_NOT_CONVERGED, DFTBGPU_ERR_FERMI, DFTBGPU_ERR_ITER_CAP, DFTBGPU_ERR_STATE, &
@@ -180,6 +180,13 @@ module dftbp_extlibs_dftbgpu
       integer(c_int), value :: enable
       integer(c_int) :: prev
     end function dftbgpu_set_fp64_emulation
+
+    !> Fp32Emulation: the FP32 eigensolves' large products as exact digit-slice tensor-core products
+    function dftbgpu_set_fp32_emulation(enable) result(prev) bind(C, name="dftbgpu_set_fp32_emulation")
+      import :: c_int
+      integer(c_int), value :: enable
+      integer(c_int) :: prev
+    end function dftbgpu_set_fp32_emulation
 
     !> TwoStage = 0 (one-stage), 1 (two-stage) or 2 (by size, the default); -1 for an invalid mode
     function dftbgpu_set_two_stage(mode) result(prev) bind(C, name="dftbgpu_set_two_stage")
