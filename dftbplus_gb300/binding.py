@@ -77,6 +77,8 @@ SIGNATURES = {
     "dftbgpu_set_two_stage": (C.c_int, [C.c_int]),
     "dftbgpu_test_twostage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_set_panel_mode": (C.c_int, [C.c_int]),
+    "dftbgpu_set_geometry_neighbours": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                  C.POINTER(C.c_int), C.c_int]),
     "dftbgpu_set_digit_gemm_kernel": (C.c_int, [C.c_int]),
     "dftbgpu_test_onestage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_test_sgemm": (C.c_int, [C.c_void_p, C.c_char, C.c_char, C.c_int, C.c_int, C.c_int, C.c_float,
@@ -176,6 +178,24 @@ class Context:
         xyz = np.ascontiguousarray(np.asarray(coords, dtype=np.float64).T)  # (N, 3): x,y,z per atom
         sp = np.ascontiguousarray(species, dtype=np.int32)
         self.check(self.lib.dftbgpu_set_geometry(self.h, len(sp), _p(xyz, C.c_double), _p(sp, C.c_int)))
+        self.natom = len(sp)
+        n = C.c_int()
+        self.check(self.lib.dftbgpu_n_orbitals(self.h, C.byref(n)))
+        self.norb = n.value
+
+    def set_geometry_neighbours(self, coords: np.ndarray, species: np.ndarray, nneigh: np.ndarray,
+                                ineigh: np.ndarray):
+        """Geometry with the host's neighbour list: nneigh[natom] neighbours within the SK cutoff per
+        atom, ineigh (natom, maxneigh + 1) their 0-based indices, column 0 the atom itself (the
+        layout of the reference's iNeighbour(0:maxNeighbour, nAtom))."""
+        xyz = np.ascontiguousarray(np.asarray(coords, dtype=np.float64).T)
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        nn = np.ascontiguousarray(nneigh, dtype=np.int32)
+        ii = np.ascontiguousarray(ineigh, dtype=np.int32)
+        if ii.ndim != 2 or ii.shape[0] != len(sp) or len(nn) != len(sp):
+            raise ValueError("ineigh must be (natom, maxneigh + 1) and nneigh (natom,)")
+        self.check(self.lib.dftbgpu_set_geometry_neighbours(self.h, len(sp), _p(xyz, C.c_double), _p(sp, C.c_int),
+                                                            _p(nn, C.c_int), _p(ii, C.c_int), ii.shape[1] - 1))
         self.natom = len(sp)
         n = C.c_int()
         self.check(self.lib.dftbgpu_n_orbitals(self.h, C.byref(n)))

@@ -1,6 +1,7 @@
 // C-ABI of the dftbgpu library: context, model/geometry upload, the SCC driver and gradients.
 // Host orchestration only; all numerical work runs in the kernels of linalg.cu, stedc.cu and
 // dftb_kernels.cu on the context's stream.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -593,7 +594,9 @@ int dftbgpu_set_model(dftbgpu_ctx *c, int nsp, const int *n_shell, const int *an
   return DFTBGPU_OK;
 }
 
-static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bool dev, const int *species) {
+// host_pi / host_pj: a half pair list (i < j, sorted) given by the caller instead of the GPU's own
+static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bool dev, const int *species,
+                             const std::vector<int> *host_pi = nullptr, const std::vector<int> *host_pj = nullptr) {
   if (!c) return DFTBGPU_ERR_ARGS;
   if (!c->have_model) return set_error(c, DFTBGPU_ERR_STATE, "set_geometry: no model set");
   if (natom <= 0 || !coords || !species) return set_error(c, DFTBGPU_ERR_ARGS, "set_geometry: bad arguments");
@@ -630,7 +633,18 @@ static int set_geometry_impl(dftbgpu_ctx *c, int natom, const double *coords, bo
   ModelDev m = model_view(c);
   // neighbour list (pairs within the SK cutoff); the pair arrays grow on demand
   int np = 0;
-  {
+  if (host_pi) {
+    np = (int)host_pi->size();
+    if (c->cap_pairs < (size_t)np || !c->d_pi) {
+      DG_CHECK(c, dev_alloc(c, &c->d_pi, (size_t)std::max(np, 1)));
+      DG_CHECK(c, dev_alloc(c, &c->d_pj, (size_t)std::max(np, 1)));
+      c->cap_pairs = (size_t)std::max(np, 1);
+    }
+    if (np > 0) {
+      DG_CUDA(c, cudaMemcpyAsync(c->d_pi, host_pi->data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+      DG_CUDA(c, cudaMemcpyAsync(c->d_pj, host_pj->data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+    }
+  } else {
     // count first to size the arrays
     size_t need = (size_t)natom * 64;
     if (c->cap_pairs < need) {
@@ -673,6 +687,37 @@ int dftbgpu_set_geometry(dftbgpu_ctx *c, int natom, const double *coords, const 
 
 int dftbgpu_set_geometry_dev(dftbgpu_ctx *c, int natom, const double *coords_dev, const int *species_host) {
   return set_geometry_impl(c, natom, coords_dev, true, species_host);
+}
+
+int dftbgpu_set_geometry_neighbours(dftbgpu_ctx *c, int natom, const double *coords, const int *species,
+                                    const int *nneigh, const int *ineigh, int maxneigh) {
+  if (!c) return DFTBGPU_ERR_ARGS;
+  if (natom <= 0 || !coords || !species || !nneigh || !ineigh || maxneigh < 0)
+    return set_error(c, DFTBGPU_ERR_ARGS, "set_geometry_neighbours: bad arguments");
+  // each pair once as (min, max), sorted like the GPU's own list
+  std::vector<long long> keys;
+  for (int i = 0; i < natom; ++i) {
+    if (nneigh[i] < 0 || nneigh[i] > maxneigh)
+      return set_error(c, DFTBGPU_ERR_ARGS, "set_geometry_neighbours: atom %d has %d neighbours (max %d)", i,
+                       nneigh[i], maxneigh);
+    const int *row = ineigh + (size_t)i * (maxneigh + 1);
+    for (int k = 1; k <= nneigh[i]; ++k) {
+      const int j = row[k];
+      if (j < 0 || j >= natom)
+        return set_error(c, DFTBGPU_ERR_ARGS,
+                         "set_geometry_neighbours: neighbour %d of atom %d is not an atom of the cluster", j, i);
+      if (j == i) continue;
+      keys.push_back((long long)std::min(i, j) * natom + std::max(i, j));
+    }
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  std::vector<int> pi(keys.size()), pj(keys.size());
+  for (size_t p = 0; p < keys.size(); ++p) {
+    pi[p] = (int)(keys[p] / natom);
+    pj[p] = (int)(keys[p] % natom);
+  }
+  return set_geometry_impl(c, natom, coords, false, species, &pi, &pj);
 }
 
 int dftbgpu_scc(dftbgpu_ctx *c, const dftbgpu_scc_opts *o, const double *q_init, dftbgpu_energies *energies,

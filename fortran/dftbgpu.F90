@@ -15,7 +15,8 @@ module dftbp_extlibs_dftbgpu
 
   public :: TDftbGpuOpts, TDftbGpuEnergies
   public :: dftbgpu_default_opts, dftbgpu_create, dftbgpu_destroy, dftbgpu_last_error
-  public :: dftbgpu_set_model, dftbgpu_set_geometry, dftbgpu_scc, dftbgpu_scc_history
+  public :: dftbgpu_set_model, dftbgpu_set_geometry, dftbgpu_set_geometry_neighbours, dftbgpu_scc
+  public :: dftbgpu_scc_history
   public :: dftbgpu_gradients, dftbgpu_n_orbitals, dftbgpu_get_orbital_populations
   public :: dftbgpu_set_tensor_cores, dftbgpu_set_fp64_emulation, dftbgpu_set_two_stage
   public :: dftbgpu_set_panel_mode, dftbgpu_set_digit_gemm_kernel, dftbgpu_set_fp32_emulation
@@ -117,6 +118,20 @@ module dftbp_extlibs_dftbgpu
       integer(c_int), intent(in) :: species(*)
       integer(c_int) :: stat
     end function dftbgpu_set_geometry
+
+    !> Geometry with the host's neighbour list (cluster case): nNeighbourSK(nAtom) and
+    !> iNeighbour(0:maxNeighbour, nAtom) of TNeighbourList (dftb/periodic.F90), passed 0-based
+    !> (iNeighbour - 1, species0 - 1); the GPU then keeps the host's pairs instead of its own
+    function dftbgpu_set_geometry_neighbours(ctx, nAtom, coords, species, nNeighbourSK, iNeighbour,&
+        & maxNeighbour) result(stat) bind(C, name="dftbgpu_set_geometry_neighbours")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nAtom
+      real(c_double), intent(in) :: coords(3, *)
+      integer(c_int), intent(in) :: species(*), nNeighbourSK(*), iNeighbour(0:maxNeighbour, *)
+      integer(c_int), value :: maxNeighbour
+      integer(c_int) :: stat
+    end function dftbgpu_set_geometry_neighbours
 
     !> SCC cycle in place of the lpSCC body (main.F90:1429-1563). qInit(nAtom) atomic populations
     !> (pass the reference q0 to start from neutral atoms); outputs as in include/dftbgpu.h

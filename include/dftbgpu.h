@@ -105,6 +105,15 @@ int dftbgpu_set_geometry(dftbgpu_ctx *ctx, int natom, const double *coords, cons
  * on the host (species_host) because the orbital layout is host metadata. */
 int dftbgpu_set_geometry_dev(dftbgpu_ctx *ctx, int natom, const double *coords_dev,
                              const int *species_host);
+/* Same with the host's neighbour list instead of the one the GPU builds from the coordinates (the
+ * cluster case of updateNeighbourListAndSpecies / getNrOfNeighboursForAll, dftb/periodic.F90:380-445
+ * and :996-1022): nneigh[natom] the neighbours of each atom within the SK cutoff (nNeighbourSK),
+ * ineigh[(maxneigh + 1) * natom] their indices laid out as iNeighbour(0:maxNeighbour, nAtom) (entry 0
+ * the atom itself), 0-based. Each pair counts once, whichever atom lists it; an index outside
+ * 0..natom-1 (a periodic image) is rejected with DFTBGPU_ERR_ARGS. Pairs beyond the SK cutoff
+ * contribute nothing; pairs within it that the list leaves out are left out of H0 and S. */
+int dftbgpu_set_geometry_neighbours(dftbgpu_ctx *ctx, int natom, const double *coords, const int *species,
+                                    const int *nneigh, const int *ineigh, int maxneigh);
 
 /*
  * SCC cycle to convergence: potentials, H = H0 + 1/2 S(V+V), generalized eigensolve, Fermi filling,
