@@ -127,9 +127,9 @@ module dftbp_extlibs_dftbgpu
       import :: c_ptr, c_int, c_double
       type(c_ptr), value :: ctx
       integer(c_int), value :: nAtom
+      integer(c_int), value :: maxNeighbour
       real(c_double), intent(in) :: coords(3, *)
       integer(c_int), intent(in) :: species(*), nNeighbourSK(*), iNeighbour(0:maxNeighbour, *)
-      integer(c_int), value :: maxNeighbour
       integer(c_int) :: stat
     end function dftbgpu_set_geometry_neighbours
 
