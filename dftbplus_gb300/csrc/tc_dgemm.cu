@@ -92,37 +92,44 @@ __device__ __forceinline__ void dg_digits(double x, int E, int *d) {
 }
 
 // ------------------------------------------------------------------------------ packing
-// One block per 32 rows of the operand (rows R, K columns; element (r, k) = src[r * rs + k * ks],
-// zero where the mask marks a structural zero: 1 keeps k <= r, 2 keeps k >= r). Pass 1 finds each
-// row's largest magnitude (written to rmax[r] as its bit pattern), pass 2 writes the eight digit
-// slabs P[s * slab + r * Kp + k] (BF16, K-major, zero-padded to Kp columns and to the block's rows).
-// 32 x 32 tiles through shared memory keep both the reads and the writes coalesced.
-__global__ void __launch_bounds__(256) dg_pack_kernel(int R, int K, const double *src, long long rs, long long ks,
-                                                      int mask, int Kp, size_t slab, __nv_bfloat16 *P,
-                                                      unsigned long long *rmax) {
-  __shared__ double tile[32][33];
-  __shared__ unsigned long long smax[32];
-  const int r0 = blockIdx.x * 32;
+// Two passes over the operand (rows R, K columns; element (r, k) = src[r * rs + k * ks], zero where
+// the mask marks a structural zero: 1 keeps k <= r, 2 keeps k >= r), each on a grid of blocks of 32
+// rows x kDgPackChunk columns, so that a square operand of a few thousand rows spreads over every
+// SM. Pass 1 (dg_rowmax_kernel) combines each row's largest magnitude into rmax[r] (its bit pattern,
+// so that unsigned order is magnitude order; rmax zeroed beforehand) with atomicMax; pass 2
+// (dg_pack_kernel) writes the eight digit slabs P[s * slab + r * Kp + k] (BF16, K-major, zero-padded
+// to Kp columns and to the block's rows). 32 x 32 tiles through shared memory keep both the reads and
+// the writes coalesced.
+constexpr int kDgPackChunk = 256;
+
+__device__ __forceinline__ void dg_load_tile(double (&tile)[32][33], int R, int K, const double *src, long long rs,
+                                             long long ks, int mask, int r0, int k0) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const bool k_contig = (ks == 1);
-  auto load_tile = [&](int k0) {
 #pragma unroll
-    for (int q = ty; q < 32; q += 8) {
-      const int r = k_contig ? r0 + q : r0 + tx;
-      const int k = k_contig ? k0 + tx : k0 + q;
-      double v = 0.0;
-      if (r < R && k < K) {
-        const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
-        if (keep) v = src[(long long)r * rs + (long long)k * ks];
-      }
-      if (k_contig) tile[q][tx] = v;
-      else tile[tx][q] = v;
+  for (int q = ty; q < 32; q += 8) {
+    const int r = k_contig ? r0 + q : r0 + tx;
+    const int k = k_contig ? k0 + tx : k0 + q;
+    double v = 0.0;
+    if (r < R && k < K) {
+      const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
+      if (keep) v = src[(long long)r * rs + (long long)k * ks];
     }
-  };
+    if (k_contig) tile[q][tx] = v;
+    else tile[tx][q] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) dg_rowmax_kernel(int R, int K, const double *src, long long rs, long long ks,
+                                                        int mask, unsigned long long *rmax) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.x * 32, kc0 = blockIdx.y * kDgPackChunk;
+  const int kc1 = min(K, kc0 + kDgPackChunk);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   unsigned long long mx[4] = {0ull, 0ull, 0ull, 0ull};
-  for (int k0 = 0; k0 < K; k0 += 32) {
+  for (int k0 = kc0; k0 < kc1; k0 += 32) {
     __syncthreads();
-    load_tile(k0);
+    dg_load_tile(tile, R, K, src, rs, ks, mask, r0, k0);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -139,16 +146,23 @@ __global__ void __launch_bounds__(256) dg_pack_kernel(int R, int K, const double
       const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
       v = w > v ? w : v;
     }
-    if (tx == 0) smax[ty + 8 * i] = v;
+    if (tx == 0 && v != 0ull) atomicMax(&rmax[r0 + ty + 8 * i], v);
   }
-  __syncthreads();
-  if (threadIdx.x < 32) rmax[r0 + threadIdx.x] = smax[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) dg_pack_kernel(int R, int K, const double *src, long long rs, long long ks,
+                                                      int mask, int Kp, size_t slab, __nv_bfloat16 *P,
+                                                      const unsigned long long *rmax) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.x * 32, kc0 = blockIdx.y * kDgPackChunk;
+  const int kc1 = min(Kp, kc0 + kDgPackChunk);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   int E[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) E[i] = dg_row_exp(smax[ty + 8 * i]);
-  for (int k0 = 0; k0 < Kp; k0 += 32) {
+  for (int i = 0; i < 4; ++i) E[i] = dg_row_exp(rmax[r0 + ty + 8 * i]);
+  for (int k0 = kc0; k0 < kc1; k0 += 32) {
     __syncthreads();
-    load_tile(k0);
+    dg_load_tile(tile, R, K, src, rs, ks, mask, r0, k0);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -659,8 +673,13 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
   const long long brs = TB ? 1 : ldb, bks = TB ? ldb : 1;
   const int amask = (flags & kALower) ? 1 : ((flags & kAUpper) ? 2 : 0);
   const int bmask = (flags & kBLower) ? 2 : ((flags & kBUpper) ? 1 : 0);
-  dg_pack_kernel<<<Mp / 32, 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, (size_t)Mp * Kp, PA, rA);
-  dg_pack_kernel<<<Np / 32, 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
+  rc = (int)cudaMemsetAsync(rA, 0, ((size_t)Mp + Np) * sizeof(unsigned long long), s);
+  if (rc != 0) return rc;
+  const int kcm = std::max(1, ceil_div(k, kDgPackChunk)), kcp = ceil_div(Kp, kDgPackChunk);
+  dg_rowmax_kernel<<<dim3(Mp / 32, kcm), 256, 0, s>>>(m, k, A, ars, aks, amask, rA);
+  dg_rowmax_kernel<<<dim3(Np / 32, kcm), 256, 0, s>>>(n, k, B, brs, bks, bmask, rB);
+  dg_pack_kernel<<<dim3(Mp / 32, kcp), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, (size_t)Mp * Kp, PA, rA);
+  dg_pack_kernel<<<dim3(Np / 32, kcp), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
   int R = 0;
   while ((1 << (R + 1)) < Kp) ++R;   // R = ceil(log2 Kp) - 1
   const int splits = dg_splits(m, n, k);
@@ -679,7 +698,7 @@ int tc_dgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, double alpha
   else
     dg_gemm_kernel<<<dim3(Mp / DG_BM, Np / DG_BN, splits), DG_THREADS, DG_SMEM, s>>>(
         m, n, Kp, Mp, Np, PA, PB, rA, rB, R, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
-  count_launch(3);
+  count_launch(5);
   if (Pp) {
     const int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
     dg_splitk_reduce<<<rb, 256, 0, s>>>(m, n, Mp, Np, splits, Pp, rA, rB, R, alpha, beta, C, ldc,

@@ -80,37 +80,43 @@ __device__ __forceinline__ void fg_digits(float x, int E, int *d) {
   }
 }
 
-// One block per 32 rows of the operand (rows R, K columns; element (r, k) = src[r * rs + k * ks], zero
-// where the mask marks a structural zero: 1 keeps k <= r, 2 keeps k >= r). Pass 1 finds each row's
-// largest magnitude (bit pattern into rmax[r]), pass 2 writes the three digit slabs P[s * slab + r *
-// Kp + k] (BF16, K-major, zero-padded to Kp columns and to the block's rows); 32 x 32 tiles through
-// shared memory keep both the reads and the writes coalesced.
-__global__ void __launch_bounds__(256) fg_pack_kernel(int R, int K, const float *src, long long rs, long long ks,
-                                                      int mask, int Kp, size_t slab, __nv_bfloat16 *P,
-                                                      unsigned *rmax) {
-  __shared__ float tile[32][33];
-  __shared__ unsigned smax[32];
-  const int r0 = blockIdx.x * 32;
+// Packing: two passes over the operand (rows R, K columns; element (r, k) = src[r * rs + k * ks], zero
+// where the mask marks a structural zero: 1 keeps k <= r, 2 keeps k >= r), each on a grid of blocks
+// of 32 rows x kFgPackChunk columns, so that a square operand of a few thousand rows spreads over
+// every SM. Pass 1 (fg_rowmax_kernel) combines each row's largest magnitude into rmax[r] (its bit
+// pattern; rmax zeroed beforehand) with atomicMax; pass 2 (fg_pack_kernel) writes the three digit
+// slabs P[s * slab + r * Kp + k] (BF16, K-major, zero-padded to Kp columns and to the block's rows).
+// 32 x 32 tiles through shared memory keep both the reads and the writes coalesced.
+constexpr int kFgPackChunk = 256;
+
+__device__ __forceinline__ void fg_load_tile(float (&tile)[32][33], int R, int K, const float *src, long long rs,
+                                             long long ks, int mask, int r0, int k0) {
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const bool k_contig = (ks == 1);
-  auto load_tile = [&](int k0) {
 #pragma unroll
-    for (int q = ty; q < 32; q += 8) {
-      const int r = k_contig ? r0 + q : r0 + tx;
-      const int k = k_contig ? k0 + tx : k0 + q;
-      float v = 0.f;
-      if (r < R && k < K) {
-        const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
-        if (keep) v = src[(long long)r * rs + (long long)k * ks];
-      }
-      if (k_contig) tile[q][tx] = v;
-      else tile[tx][q] = v;
+  for (int q = ty; q < 32; q += 8) {
+    const int r = k_contig ? r0 + q : r0 + tx;
+    const int k = k_contig ? k0 + tx : k0 + q;
+    float v = 0.f;
+    if (r < R && k < K) {
+      const bool keep = (mask == 0) || (mask == 1 && k <= r) || (mask == 2 && k >= r);
+      if (keep) v = src[(long long)r * rs + (long long)k * ks];
     }
-  };
+    if (k_contig) tile[q][tx] = v;
+    else tile[tx][q] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) fg_rowmax_kernel(int R, int K, const float *src, long long rs, long long ks,
+                                                        int mask, unsigned *rmax) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, kc0 = blockIdx.y * kFgPackChunk;
+  const int kc1 = min(K, kc0 + kFgPackChunk);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   unsigned mx[4] = {0u, 0u, 0u, 0u};
-  for (int k0 = 0; k0 < K; k0 += 32) {
+  for (int k0 = kc0; k0 < kc1; k0 += 32) {
     __syncthreads();
-    load_tile(k0);
+    fg_load_tile(tile, R, K, src, rs, ks, mask, r0, k0);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -126,16 +132,23 @@ __global__ void __launch_bounds__(256) fg_pack_kernel(int R, int K, const float 
       const unsigned w = __shfl_xor_sync(0xffffffffu, v, o);
       v = w > v ? w : v;
     }
-    if (tx == 0) smax[ty + 8 * i] = v;
+    if (tx == 0 && v != 0u) atomicMax(&rmax[r0 + ty + 8 * i], v);
   }
-  __syncthreads();
-  if (threadIdx.x < 32) rmax[r0 + threadIdx.x] = smax[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) fg_pack_kernel(int R, int K, const float *src, long long rs, long long ks,
+                                                      int mask, int Kp, size_t slab, __nv_bfloat16 *P,
+                                                      const unsigned *rmax) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, kc0 = blockIdx.y * kFgPackChunk;
+  const int kc1 = min(Kp, kc0 + kFgPackChunk);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   int E[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) E[i] = fg_row_exp(smax[ty + 8 * i]);
-  for (int k0 = 0; k0 < Kp; k0 += 32) {
+  for (int i = 0; i < 4; ++i) E[i] = fg_row_exp(rmax[r0 + ty + 8 * i]);
+  for (int k0 = kc0; k0 < kc1; k0 += 32) {
     __syncthreads();
-    load_tile(k0);
+    fg_load_tile(tile, R, K, src, rs, ks, mask, r0, k0);
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -359,7 +372,7 @@ __global__ void fg_splitk_reduce(int m, int n, int Mp, int Np, int splits, const
 // ------------------------------------------------------------------------------ host side
 thread_local bool g_tc_fgemm = false;          // gemm<float> routes here while set (calling thread only)
 std::atomic<bool> g_tc_fgemm_mixed{true};      // dftbgpu_set_fp32_digit_products
-constexpr int kFgSMs = 148;
+constexpr int kFgSMs = 148;   // CTAs in flight (one per SM; GB300 has 152, a few may be taken)
 static thread_local ThreadScratch t_fg;
 enum { kFgSlabs = 0, kFgRmax = 1, kFgPart = 2 };
 
@@ -395,8 +408,13 @@ int tc_fgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha,
   const long long brs = TB ? 1 : ldb, bks = TB ? ldb : 1;
   const int amask = (flags & kALower) ? 1 : ((flags & kAUpper) ? 2 : 0);
   const int bmask = (flags & kBLower) ? 2 : ((flags & kBUpper) ? 1 : 0);
-  fg_pack_kernel<<<Mp / 32, 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, (size_t)Mp * Kp, PA, rA);
-  fg_pack_kernel<<<Np / 32, 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
+  rc = (int)cudaMemsetAsync(rA, 0, ((size_t)Mp + Np) * sizeof(unsigned), s);
+  if (rc != 0) return rc;
+  const int kcm = std::max(1, ceil_div(k, kFgPackChunk)), kcp = ceil_div(Kp, kFgPackChunk);
+  fg_rowmax_kernel<<<dim3(Mp / 32, kcm), 256, 0, s>>>(m, k, A, ars, aks, amask, rA);
+  fg_rowmax_kernel<<<dim3(Np / 32, kcm), 256, 0, s>>>(n, k, B, brs, bks, bmask, rB);
+  fg_pack_kernel<<<dim3(Mp / 32, kcp), 256, 0, s>>>(m, k, A, ars, aks, amask, Kp, (size_t)Mp * Kp, PA, rA);
+  fg_pack_kernel<<<dim3(Np / 32, kcp), 256, 0, s>>>(n, k, B, brs, bks, bmask, Kp, (size_t)Np * Kp, PB, rB);
   const int splits = fg_splits(m, n, k);
   long long *Pp = nullptr;
   int kb_split = 0;
@@ -408,7 +426,7 @@ int tc_fgemm(cudaStream_t s, char ta, char tb, int m, int n, int k, float alpha,
   }
   fg_gemm_kernel<<<dim3(Mp / FG_BM, Np / FG_BN, splits), FG_THREADS, FG_SMEM, s>>>(
       m, n, Kp, Mp, Np, PA, PB, rA, rB, alpha, beta, C, ldc, flags, ds.err, Pp, kb_split);
-  count_launch(3);
+  count_launch(5);
   if (Pp) {
     const int rb = (int)std::min<long long>(((long long)m * n + 255) / 256, 152 * 8);
     fg_splitk_reduce<<<rb, 256, 0, s>>>(m, n, Mp, Np, splits, Pp, rA, rB, alpha, beta, C, ldc,
