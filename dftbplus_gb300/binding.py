@@ -77,6 +77,7 @@ SIGNATURES = {
     "dftbgpu_set_two_stage": (C.c_int, [C.c_int]),
     "dftbgpu_test_twostage": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int, _dp, _dp, _dp]),
     "dftbgpu_set_panel_mode": (C.c_int, [C.c_int]),
+    "dftbgpu_set_dc_staging": (C.c_int, [C.c_int]),
     "dftbgpu_set_geometry_neighbours": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                                   C.POINTER(C.c_int), C.c_int]),
     "dftbgpu_set_digit_gemm_kernel": (C.c_int, [C.c_int]),
@@ -465,6 +466,13 @@ def set_panel_mode(mode) -> int:
     if prev < 0:
         raise ValueError(f"panel mode {mode!r}: expected 0, 1 or 2")
     return prev
+
+
+def set_dc_staging(enable: bool) -> bool:
+    """Deflation of the tridiagonal divide and conquer (process-wide): True (the default) stages each
+    merge that fits in shared memory, False runs every merge in global memory. Returns the previous
+    setting."""
+    return bool(load_library().dftbgpu_set_dc_staging(1 if enable else 0))
 
 
 def set_two_stage(mode) -> int:

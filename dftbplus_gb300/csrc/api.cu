@@ -1063,6 +1063,8 @@ int dftbgpu_set_panel_mode(int mode) {
   return g_panel_mode.exchange(mode);
 }
 
+int dftbgpu_set_dc_staging(int enable) { return g_dc_stage.exchange(enable ? 1 : 0); }
+
 int dftbgpu_set_fp64_emulation(int enable) {
   const int prev = g_tc_dgemm_mixed ? 1 : 0;
   g_tc_dgemm_mixed = enable != 0;

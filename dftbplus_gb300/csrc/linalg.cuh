@@ -162,6 +162,10 @@ void larft(cudaStream_t s, int nb, const T *G, const T *tau, T *Tf);
 // work: stedc_work_size(n) elements of T, iwork: stedc_iwork_size(n) ints.
 size_t stedc_work_size(int n);
 size_t stedc_iwork_size(int n);
+// Deflation of stedc's merges (process-wide): 1 (default) stages every merge that fits in shared
+// memory (sequential scan at shared-memory latency, parallel compaction); 0 runs every merge's scan
+// and compaction in global memory by one thread (the path merges above the staging limit take).
+extern std::atomic<int> g_dc_stage;
 template <typename T>
 int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork, int *status_dev);
 

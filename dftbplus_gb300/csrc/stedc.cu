@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <atomic>
+
 #include "linalg.cuh"
 
 namespace dg {
@@ -122,9 +124,60 @@ __global__ void dc_sort_kernel(const Merge *merges, const T *d, const T *e, cons
   }
 }
 
-// K2: deflation (sequential scan by one thread after a parallel max reduction).
+// K2: deflation. The scan over the sorted entries is sequential (a rotation changes the z entry and
+// the pole the next test reads), so one thread runs it after a parallel max reduction. Scan: an
+// entry with negligible rho |z_j| deflates; otherwise, against the previous surviving entry, a
+// rotation that zeroes z_prev deflates the pair when |(d_j - d_prev) c s| is negligible. F is the
+// flag type (1 = deflated); the rotations go to W.rot_cols / W.rot_cs at the merge's offset a.
+template <typename T, typename F>
+__device__ int dc_deflate_scan(int N, int a, T *Ds, T *zs, const int *perm, F *flag, T rho2, T mz, T tol,
+                               const DcWork<T> &W) {
+  int nrot = 0;
+  for (int j = 0; j < N; ++j) flag[j] = 0;
+  if (rho2 * mz <= tol) {
+    for (int j = 0; j < N; ++j) flag[j] = 1;
+    return 0;
+  }
+  int prev = -1;
+  for (int j = 0; j < N; ++j) {
+    if (rho2 * fabs(zs[j]) <= tol) {
+      flag[j] = 1;
+      continue;
+    }
+    if (prev >= 0) {
+      T s = zs[prev], c = zs[j];
+      T t = t_hypot(c, s);
+      T tdiff = Ds[j] - Ds[prev];
+      c /= t;
+      s = -s / t;
+      if (fabs(tdiff * c * s) <= tol) {
+        zs[j] = t;
+        zs[prev] = T(0);
+        W.rot_cols[2 * (a + nrot)] = a + perm[prev];
+        W.rot_cols[2 * (a + nrot) + 1] = a + perm[j];
+        W.rot_cs[2 * (a + nrot)] = c;
+        W.rot_cs[2 * (a + nrot) + 1] = s;
+        ++nrot;
+        T tt = Ds[prev] * c * c + Ds[j] * s * s;
+        Ds[j] = Ds[prev] * s * s + Ds[j] * c * c;
+        Ds[prev] = tt;
+        flag[prev] = 1;
+      }
+    }
+    prev = j;
+  }
+  return nrot;
+}
+
+// One CTA per merge. A merge of at most stage_n entries is staged in dynamic shared memory (its
+// sorted poles, z entries, origins and flags: N (2 sizeof(T) + 5) bytes), so each step of the scan
+// costs shared-memory latency instead of global round trips, and the compaction (non-deflated
+// positions -> ndpos with their poles and z entries in dl / w, deflated positions -> dfpos, both in
+// order) is a CTA-wide prefix sum; the staged poles and z entries are written back. A larger merge
+// runs the scan and the compaction in global memory by one thread.
 template <typename T>
-__global__ void dc_deflate_kernel(const Merge *merges, const T *e, DcWork<T> W) {
+__global__ void __launch_bounds__(256) dc_deflate_kernel(const Merge *merges, const T *e, DcWork<T> W, int stage_n) {
+  extern __shared__ __align__(16) unsigned char dc_dsm[];
   const int mi = blockIdx.x;
   Merge mg = merges[mi];
   if (mg.m == mg.b) {
@@ -132,79 +185,121 @@ __global__ void dc_deflate_kernel(const Merge *merges, const T *e, DcWork<T> W) 
     return;
   }
   const int a = mg.a, N = mg.b - mg.a;
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5;
+  const bool staged = N <= stage_n;
   __shared__ T smax[2][32];
+  __shared__ int s_scan[32];
+  __shared__ int s_nrot;
   T md = T(0), mz = T(0);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  for (int i = t; i < N; i += nt) {
     md = fmax(md, fabs(W.Ds[a + i]));
     mz = fmax(mz, fabs(W.zs[a + i]));
   }
   md = wmax(md);
   mz = wmax(mz);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) { smax[0][wid] = md; smax[1][wid] = mz; }
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-    md = fmax(md, smax[0][k]);
-    mz = fmax(mz, smax[1][k]);
-  }
-  md = fmax(md, smax[0][0]);
-  mz = fmax(mz, smax[1][0]);
-  const T rho2 = T(2) * fabs(e[mg.m - 1]);
-  const T tol = T(8) * Lim<T>::eps * fmax(md, mz);
-  T *Ds = W.Ds + a, *zs = W.zs + a;
-  int *perm = W.perm + a;
-  int nrot = 0, K = 0, nD = 0;
-  // flags are kept in ndpos temporarily: 1 = deflated
-  int *flag = W.dfpos + a;
-  for (int j = 0; j < N; ++j) flag[j] = 0;
-  if (rho2 * mz <= tol) {
-    for (int j = 0; j < N; ++j) flag[j] = 1;
-  } else {
-    int prev = -1;
-    for (int j = 0; j < N; ++j) {
-      if (rho2 * fabs(zs[j]) <= tol) {
-        flag[j] = 1;
-        continue;
-      }
-      if (prev >= 0) {
-        T s = zs[prev], c = zs[j];
-        T t = t_hypot(c, s);
-        T tdiff = Ds[j] - Ds[prev];
-        c /= t;
-        s = -s / t;
-        if (fabs(tdiff * c * s) <= tol) {
-          zs[j] = t;
-          zs[prev] = T(0);
-          W.rot_cols[2 * (a + nrot)] = a + perm[prev];
-          W.rot_cols[2 * (a + nrot) + 1] = a + perm[j];
-          W.rot_cs[2 * (a + nrot)] = c;
-          W.rot_cs[2 * (a + nrot) + 1] = s;
-          ++nrot;
-          T tt = Ds[prev] * c * c + Ds[j] * s * s;
-          Ds[j] = Ds[prev] * s * s + Ds[j] * c * c;
-          Ds[prev] = tt;
-          flag[prev] = 1;
-        }
-      }
-      prev = j;
+  T *sD = reinterpret_cast<T *>(dc_dsm), *sZ = sD + N;
+  int *sP = reinterpret_cast<int *>(sZ + N);
+  unsigned char *sF = reinterpret_cast<unsigned char *>(sP + N);
+  if (staged) {
+    for (int i = t; i < N; i += nt) {
+      sD[i] = W.Ds[a + i];
+      sZ[i] = W.zs[a + i];
+      sP[i] = W.perm[a + i];
     }
   }
-  // compact: non-deflated positions -> ndpos, deflated -> dfpos (overwrites the flags in order,
-  // safe because dfpos[t] is written only after flag[j] with j >= t has been read)
-  for (int j = 0; j < N; ++j) {
-    if (!flag[j]) {
+  __syncthreads();
+  if (t == 0) {
+    for (int k = 1; k < (nt >> 5); ++k) {
+      md = fmax(md, smax[0][k]);
+      mz = fmax(mz, smax[1][k]);
+    }
+    md = fmax(md, smax[0][0]);
+    mz = fmax(mz, smax[1][0]);
+    const T rho2 = T(2) * fabs(e[mg.m - 1]);
+    const T tol = T(8) * Lim<T>::eps * fmax(md, mz);
+    if (staged) {
+      s_nrot = dc_deflate_scan(N, a, sD, sZ, sP, sF, rho2, mz, tol, W);
+    } else {
+      // flags kept in dfpos temporarily; the sequential compaction overwrites them in order (dfpos[q]
+      // is written only after flag[j] with j >= q has been read)
+      T *Ds = W.Ds + a, *zs = W.zs + a;
+      int *flag = W.dfpos + a;
+      const int nrot = dc_deflate_scan(N, a, Ds, zs, W.perm + a, flag, rho2, mz, tol, W);
+      int K = 0, nD = 0;
+      for (int j = 0; j < N; ++j) {
+        if (!flag[j]) {
+          W.ndpos[a + K] = j;
+          W.dl[a + K] = Ds[j];
+          W.w[a + K] = zs[j];
+          ++K;
+        } else {
+          flag[nD] = j;
+          ++nD;
+        }
+      }
+      W.mK[mi] = K;
+      W.mRot[mi] = nrot;
+    }
+  }
+  if (!staged) return;
+  __syncthreads();
+  // compaction: thread t takes the contiguous chunk [j0, j1); exclusive prefix sum of the surviving
+  // counts over the threads
+  const int C = (N + nt - 1) / nt;
+  const int j0 = min(N, t * C), j1 = min(N, j0 + C);
+  int cnt = 0;
+  for (int j = j0; j < j1; ++j) cnt += sF[j] ? 0 : 1;
+  int inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  if (lane == 31) s_scan[wid] = inc;
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int w = 0; w < (nt >> 5); ++w) {
+      const int v = s_scan[w];
+      s_scan[w] = run;
+      run += v;
+    }
+    W.mK[mi] = run;
+    W.mRot[mi] = s_nrot;
+  }
+  __syncthreads();
+  int K = s_scan[wid] + inc - cnt;   // surviving entries before j0
+  int nD = j0 - K;                   // deflated entries before j0
+  for (int j = j0; j < j1; ++j) {
+    if (!sF[j]) {
       W.ndpos[a + K] = j;
-      W.dl[a + K] = Ds[j];
-      W.w[a + K] = zs[j];
+      W.dl[a + K] = sD[j];
+      W.w[a + K] = sZ[j];
       ++K;
     } else {
-      flag[nD] = j;
+      W.dfpos[a + nD] = j;
       ++nD;
     }
   }
-  W.mK[mi] = K;
-  W.mRot[mi] = nrot;
+  for (int i = t; i < N; i += nt) {
+    W.Ds[a + i] = sD[i];
+    W.zs[a + i] = sZ[i];
+  }
+}
+
+// Largest merge staged by dc_deflate_kernel and its dynamic shared memory (bytes) for a level whose
+// largest block has max_block entries: the merge fits below kDcStageBytes or nothing is staged.
+constexpr int kDcStageBytes = 160 * 1024;
+std::atomic<int> g_dc_stage{1};
+template <typename T>
+static int dc_stage_n(int max_block) {
+  if (!g_dc_stage.load(std::memory_order_relaxed)) return 0;
+  return (size_t)max_block * (2 * sizeof(T) + 5) <= (size_t)kDcStageBytes ? max_block : 0;
+}
+template <typename T>
+static size_t dc_stage_bytes(int stage_n) {
+  return (size_t)stage_n * (2 * sizeof(T) + 5);
 }
 
 // K3: apply the recorded rotations to the Q columns (each thread owns a row of the block).
@@ -576,7 +671,15 @@ int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork,
     const int *pma = dev_meta + off_pma[li];
     int nm = (int)L.merges.size();
     dc_sort_kernel<T><<<nm, 256, 0, s>>>(dm, d, e, Qin, ldq, W);
-    dc_deflate_kernel<T><<<nm, 256, 0, s>>>(dm, e, W);
+    {
+      static bool attr = false;   // per instantiation: the largest staging size, set once
+      if (!attr) {
+        cudaFuncSetAttribute(dc_deflate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDcStageBytes);
+        attr = true;
+      }
+      const int sn = dc_stage_n<T>(L.max_block);
+      dc_deflate_kernel<T><<<nm, 256, dc_stage_bytes<T>(sn), s>>>(dm, e, W, sn);
+    }
     dim3 gr(nm, ceil_div(L.max_block, 256));
     dc_rotate_kernel<T><<<gr, 256, 0, s>>>(dm, Qin, ldq, W);
     int warps_blocks = ceil_div((long long)n * 32, 256);
@@ -703,7 +806,8 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
     const int nm = P.nm[L];
     const int max_block = std::min(1 << L, n);
     dc_sort_kernel<double><<<nm, 256, 0, s>>>(dm, d, e, Qin, n, W);
-    dc_deflate_kernel<double><<<nm, 256, 0, s>>>(dm, e, W);
+    const int sn = dc_stage_n<double>(max_block);   // max_block <= 256: under the default 48 KB
+    dc_deflate_kernel<double><<<nm, 256, dc_stage_bytes<double>(sn), s>>>(dm, e, W, sn);
     dim3 gr(nm, ceil_div(max_block, 256));
     dc_rotate_kernel<double><<<gr, 256, 0, s>>>(dm, Qin, n, W);
     int wb = ceil_div((long long)n * 32, 256);

@@ -20,6 +20,7 @@ module dftbp_extlibs_dftbgpu
   public :: dftbgpu_gradients, dftbgpu_n_orbitals, dftbgpu_get_orbital_populations
   public :: dftbgpu_set_tensor_cores, dftbgpu_set_fp64_emulation, dftbgpu_set_two_stage
   public :: dftbgpu_set_panel_mode, dftbgpu_set_digit_gemm_kernel, dftbgpu_set_fp32_emulation
+  public :: dftbgpu_set_dc_staging
   public :: dftbgpuErrorMessage
   public :: DFTBGPU_OK, DFTBGPU_ERR_ARGS, DFTBGPU_ERR_CUDA, DFTBGPU_ERR_NOT_POSDEF, &
       & DFTBGPU_ERR_SCC_NOT_CONVERGED, DFTBGPU_ERR_FERMI, DFTBGPU_ERR_ITER_CAP, DFTBGPU_ERR_STATE, &
@@ -217,6 +218,14 @@ module dftbp_extlibs_dftbgpu
       integer(c_int), value :: mode
       integer(c_int) :: prev
     end function dftbgpu_set_panel_mode
+
+    !> DcStaging = 1 (merges of the tridiagonal divide and conquer deflated in shared memory where
+    !> they fit, the default) or 0 (all in global memory); returns the previous setting
+    function dftbgpu_set_dc_staging(enable) result(prev) bind(C, name="dftbgpu_set_dc_staging")
+      import :: c_int
+      integer(c_int), value :: enable
+      integer(c_int) :: prev
+    end function dftbgpu_set_dc_staging
 
     !> Fp64EmulationKernel = 0 (single-stage, the default) or 1 (TMA-pipelined); -1 for an invalid mode
     function dftbgpu_set_digit_gemm_kernel(mode) result(prev) bind(C, name="dftbgpu_set_digit_gemm_kernel")

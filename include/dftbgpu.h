@@ -315,6 +315,15 @@ int dftbgpu_set_two_stage(int mode);
  * path at small sizes). Process-wide; returns the previous mode, or -1 for an invalid mode.
  */
 int dftbgpu_set_panel_mode(int mode);
+/*
+ * Deflation step of the tridiagonal divide and conquer (no reference counterpart; the reference
+ * calls LAPACK dstedc/MAGMA): enable = 1 (the default) stages each merge that fits (up to 160 KB of
+ * shared memory: 6,144+ entries in FP64, 12,000+ in FP32) on chip, so the sequential deflation scan
+ * runs at shared-memory latency and the compaction is a parallel prefix sum; 0 runs every merge in
+ * global memory by one thread, as larger merges always do. Same results either way. Process-wide;
+ * returns the previous setting.
+ */
+int dftbgpu_set_dc_staging(int enable);
 int dftbgpu_test_dgemm_tc(dftbgpu_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha, const double *a,
                           int lda, const double *b, int ldb, double beta, double *c, int ldc, int flags);
 /*
