@@ -8,7 +8,11 @@
 //   secular : 1 + rho sum w_j^2 / (d_j - lambda) = 0, one warp per root, bracketed two-pole
 //             rational iteration with bisection safeguard (bounded iterations, status on cap)
 //   zhat    : z_j^2 = prod_i (lambda_i - d_j) / (rho prod_{i != j} (d_i - d_j))
-//   vectors : U(:, i) = zhat / (d - lambda_i), normalised; Q_new = Q_nondeflated * U (GEMM)
+//   vectors : U(:, i) = zhat / (d - lambda_i), normalised; Q_new = Q_nondeflated * U as two GEMMs,
+//             one per half of the rows: the surviving columns are grouped by row support (left
+//             half only, both halves after a rotation across the halves, right half only), and
+//             each half multiplies only the groups that are non-zero in it (half the FLOPs when no
+//             rotation crosses the halves)
 //   scatter : final ascending order of roots and deflated values, columns placed accordingly.
 // This replaces the tridiagonal stage of dsygvd (math/eigensolver.F90:561-660 'D' solvers).
 #include <algorithm>
@@ -32,6 +36,10 @@ template <typename T>
 struct DcWork {
   T *Ds, *zs, *dl, *w, *tau, *lam, *zh, *rot_cs, *vals;
   int *perm, *ndpos, *dfpos, *org, *rot_cols, *mK, *mRot, *srcinfo;
+  // grp[a + k]: column of the surviving pole k in the type-grouped order of the merge product (rows
+  // of U, columns of Gs): columns supported on the left half only, then on both halves (a rotation
+  // across the halves), then on the right half only; mK1 / mK2 per merge: the first two group ends
+  int *grp, *mK1, *mK2;
   T *Gs, *U, *Qtmp, *Qalt;
 };
 
@@ -128,12 +136,20 @@ __global__ void dc_sort_kernel(const Merge *merges, const T *d, const T *e, cons
 // the pole the next test reads), so one thread runs it after a parallel max reduction. Scan: an
 // entry with negligible rho |z_j| deflates; otherwise, against the previous surviving entry, a
 // rotation that zeroes z_prev deflates the pair when |(d_j - d_prev) c s| is negligible. F is the
-// flag type (1 = deflated); the rotations go to W.rot_cols / W.rot_cs at the merge's offset a.
-template <typename T, typename F>
-__device__ int dc_deflate_scan(int N, int a, T *Ds, T *zs, const int *perm, F *flag, T rho2, T mz, T tol,
-                               const DcWork<T> &W) {
+// flag type (1 = deflated); the rotations go to W.rot_cols / W.rot_cs at the merge's offset a. sup
+// tracks the row support of each entry's column (1 left half, 2 right half, 3 both after a rotation
+// across the halves); the first nL of the merge's N original columns are the left half's.
+// Group of a surviving column by its row support: 0 left half only, 1 both halves, 2 right half only.
+__device__ __forceinline__ int dc_sup_type(int sup) { return sup == 1 ? 0 : (sup == 3 ? 1 : 2); }
+
+template <typename T, typename F, typename S>
+__device__ int dc_deflate_scan(int N, int nL, int a, T *Ds, T *zs, const int *perm, F *flag, S *sup, T rho2, T mz,
+                               T tol, const DcWork<T> &W) {
   int nrot = 0;
-  for (int j = 0; j < N; ++j) flag[j] = 0;
+  for (int j = 0; j < N; ++j) {
+    flag[j] = 0;
+    sup[j] = (perm[j] < nL) ? 1 : 2;   // row support of the entry's column: 1 left half, 2 right half
+  }
   if (rho2 * mz <= tol) {
     for (int j = 0; j < N; ++j) flag[j] = 1;
     return 0;
@@ -162,6 +178,7 @@ __device__ int dc_deflate_scan(int N, int a, T *Ds, T *zs, const int *perm, F *f
         Ds[j] = Ds[prev] * s * s + Ds[j] * c * c;
         Ds[prev] = tt;
         flag[prev] = 1;
+        sup[j] = sup[j] | sup[prev];
       }
     }
     prev = j;
@@ -170,11 +187,12 @@ __device__ int dc_deflate_scan(int N, int a, T *Ds, T *zs, const int *perm, F *f
 }
 
 // One CTA per merge. A merge of at most stage_n entries is staged in dynamic shared memory (its
-// sorted poles, z entries, origins and flags: N (2 sizeof(T) + 5) bytes), so each step of the scan
+// sorted poles, z entries, origins, flags and supports: N (2 sizeof(T) + 6) bytes), so each step of the scan
 // costs shared-memory latency instead of global round trips, and the compaction (non-deflated
 // positions -> ndpos with their poles and z entries in dl / w, deflated positions -> dfpos, both in
-// order) is a CTA-wide prefix sum; the staged poles and z entries are written back. A larger merge
-// runs the scan and the compaction in global memory by one thread.
+// order; the support type of each survivor, 0 left / 1 both / 2 right, to grp) is a CTA-wide prefix
+// sum; the staged poles and z entries are written back. A larger merge runs the scan and the
+// compaction in global memory by one thread.
 template <typename T>
 __global__ void __launch_bounds__(256) dc_deflate_kernel(const Merge *merges, const T *e, DcWork<T> W, int stage_n) {
   extern __shared__ __align__(16) unsigned char dc_dsm[];
@@ -200,7 +218,7 @@ __global__ void __launch_bounds__(256) dc_deflate_kernel(const Merge *merges, co
   if (lane == 0) { smax[0][wid] = md; smax[1][wid] = mz; }
   T *sD = reinterpret_cast<T *>(dc_dsm), *sZ = sD + N;
   int *sP = reinterpret_cast<int *>(sZ + N);
-  unsigned char *sF = reinterpret_cast<unsigned char *>(sP + N);
+  unsigned char *sF = reinterpret_cast<unsigned char *>(sP + N), *sS = sF + N;
   if (staged) {
     for (int i = t; i < N; i += nt) {
       sD[i] = W.Ds[a + i];
@@ -218,20 +236,23 @@ __global__ void __launch_bounds__(256) dc_deflate_kernel(const Merge *merges, co
     mz = fmax(mz, smax[1][0]);
     const T rho2 = T(2) * fabs(e[mg.m - 1]);
     const T tol = T(8) * Lim<T>::eps * fmax(md, mz);
+    const int nL = mg.m - mg.a;
     if (staged) {
-      s_nrot = dc_deflate_scan(N, a, sD, sZ, sP, sF, rho2, mz, tol, W);
+      s_nrot = dc_deflate_scan(N, nL, a, sD, sZ, sP, sF, sS, rho2, mz, tol, W);
     } else {
-      // flags kept in dfpos temporarily; the sequential compaction overwrites them in order (dfpos[q]
-      // is written only after flag[j] with j >= q has been read)
+      // flags kept in dfpos and supports in grp temporarily; the sequential compaction overwrites both
+      // in order (dfpos[q] and grp[q] are written only after entry j >= q has been read)
       T *Ds = W.Ds + a, *zs = W.zs + a;
-      int *flag = W.dfpos + a;
-      const int nrot = dc_deflate_scan(N, a, Ds, zs, W.perm + a, flag, rho2, mz, tol, W);
+      int *flag = W.dfpos + a, *sup = W.grp + a;
+      const int nrot = dc_deflate_scan(N, nL, a, Ds, zs, W.perm + a, flag, sup, rho2, mz, tol, W);
       int K = 0, nD = 0;
       for (int j = 0; j < N; ++j) {
         if (!flag[j]) {
+          const int sj = sup[j];
           W.ndpos[a + K] = j;
           W.dl[a + K] = Ds[j];
           W.w[a + K] = zs[j];
+          W.grp[a + K] = dc_sup_type(sj);
           ++K;
         } else {
           flag[nD] = j;
@@ -276,6 +297,7 @@ __global__ void __launch_bounds__(256) dc_deflate_kernel(const Merge *merges, co
       W.ndpos[a + K] = j;
       W.dl[a + K] = sD[j];
       W.w[a + K] = sZ[j];
+      W.grp[a + K] = dc_sup_type(sS[j]);
       ++K;
     } else {
       W.dfpos[a + nD] = j;
@@ -295,11 +317,72 @@ std::atomic<int> g_dc_stage{1};
 template <typename T>
 static int dc_stage_n(int max_block) {
   if (!g_dc_stage.load(std::memory_order_relaxed)) return 0;
-  return (size_t)max_block * (2 * sizeof(T) + 5) <= (size_t)kDcStageBytes ? max_block : 0;
+  return (size_t)max_block * (2 * sizeof(T) + 6) <= (size_t)kDcStageBytes ? max_block : 0;
 }
 template <typename T>
 static size_t dc_stage_bytes(int stage_n) {
-  return (size_t)stage_n * (2 * sizeof(T) + 5);
+  return (size_t)stage_n * (2 * sizeof(T) + 6);
+}
+
+// K2b: positions of the surviving poles in the type-grouped order of the merge product (stable within
+// each group), from the types the deflation left in grp; one CTA per merge, prefix sums of the three
+// counts over contiguous chunks. mK1 / mK2 receive the ends of the first two groups.
+template <typename T>
+__global__ void __launch_bounds__(256) dc_group_kernel(const Merge *merges, DcWork<T> W) {
+  const int mi = blockIdx.x;
+  Merge mg = merges[mi];
+  if (mg.m == mg.b) return;
+  const int a = mg.a, K = W.mK[mi];
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5, nw = nt >> 5;
+  __shared__ int s_c[3][33];
+  const int C = (K + nt - 1) / nt;
+  const int k0 = min(K, t * C), k1 = min(K, k0 + C);
+  int c0 = 0, c1 = 0, c2 = 0;
+  for (int k = k0; k < k1; ++k) {
+    const int ty = W.grp[a + k];
+    c0 += (ty == 0);
+    c1 += (ty == 1);
+    c2 += (ty == 2);
+  }
+  int i0 = c0, i1 = c1, i2 = c2;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v0 = __shfl_up_sync(0xffffffffu, i0, o);
+    const int v1 = __shfl_up_sync(0xffffffffu, i1, o);
+    const int v2 = __shfl_up_sync(0xffffffffu, i2, o);
+    if (lane >= o) {
+      i0 += v0;
+      i1 += v1;
+      i2 += v2;
+    }
+  }
+  if (lane == 31) {
+    s_c[0][wid] = i0;
+    s_c[1][wid] = i1;
+    s_c[2][wid] = i2;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int q = 0; q < 3; ++q) {
+      int run = 0;
+      for (int w = 0; w < nw; ++w) {
+        const int v = s_c[q][w];
+        s_c[q][w] = run;
+        run += v;
+      }
+      s_c[q][32] = run;
+    }
+    W.mK1[mi] = s_c[0][32];
+    W.mK2[mi] = s_c[0][32] + s_c[1][32];
+  }
+  __syncthreads();
+  int p0 = s_c[0][wid] + i0 - c0;
+  int p1 = s_c[0][32] + s_c[1][wid] + i1 - c1;
+  int p2 = s_c[0][32] + s_c[1][32] + s_c[2][wid] + i2 - c2;
+  for (int k = k0; k < k1; ++k) {
+    const int ty = W.grp[a + k];
+    W.grp[a + k] = (ty == 0) ? p0++ : ((ty == 1) ? p1++ : p2++);
+  }
 }
 
 // K3: apply the recorded rotations to the Q columns (each thread owns a row of the block).
@@ -464,7 +547,8 @@ __global__ void dc_zhat_kernel(int n, const Merge *merges, const int *pos_merge,
   }
 }
 
-// K6: eigenvector matrix of the rank-one problem, one warp per column i; U rows [0,K) at column a+i.
+// K6: eigenvector matrix of the rank-one problem, one warp per column i; U rows [0,K) at column a+i,
+// row grp[a + t] for pole t (the type-grouped order of the merge product).
 template <typename T>
 __global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_merge, DcWork<T> W, int ldu) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -484,14 +568,15 @@ __global__ void dc_build_u_kernel(int n, const Merge *merges, const int *pos_mer
   T s = T(0);
   for (int t = lane; t < K; t += 32) {
     T v = W.zh[a + t] / ((dl[t] - dorg) - tau);
-    u[t] = v;
+    u[W.grp[a + t]] = v;
     s += v * v;
   }
   T inv = T(1) / sqrt(wsum(s));
   for (int t = lane; t < K; t += 32) u[t] *= inv;
 }
 
-// K7: gather the non-deflated Q columns (rows [a,b)) into Gs at columns a .. a+K-1.
+// K7: gather the non-deflated Q columns (rows [a,b)) into Gs at columns a .. a+K-1, pole t at column
+// a + grp[a + t].
 template <typename T>
 __global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merge, const T *Q, int ldq,
                                  DcWork<T> W, int ldg) {
@@ -503,9 +588,9 @@ __global__ void dc_gather_kernel(int n, const Merge *merges, const int *pos_merg
   const int K = W.mK[mi];
   const int t = g - a;
   if (t >= K) return;
-  int src = a + W.perm[a + W.ndpos[a + t]];
-  for (int r = mg.a + threadIdx.x; r < mg.b; r += blockDim.x)
-    W.Gs[r + (size_t)g * ldg] = Q[r + (size_t)src * ldq];
+  const int src = a + W.perm[a + W.ndpos[a + t]];
+  const size_t dst = (size_t)(a + W.grp[a + t]) * ldg;
+  for (int r = mg.a + threadIdx.x; r < mg.b; r += blockDim.x) W.Gs[r + dst] = Q[r + (size_t)src * ldq];
 }
 
 // K8 (small merges): Qtmp[a:b, a:a+K] = Gs[a:b, a:a+K] * U[0:K, a:a+K] inside one CTA.
@@ -614,8 +699,19 @@ size_t stedc_work_size(int n) {
 size_t stedc_iwork_size(int n) {
   int levels = 0;
   while ((1LL << levels) < n) ++levels;
-  // 10 n index vectors + plan metadata (bounds n, merges 4 n, two position maps per level)
-  return (size_t)n * (10 + 1 + 4 + 2 * (size_t)(levels + 1)) + 64;
+  // 13 n index vectors + plan metadata (bounds n, merges 4 n, two position maps per level)
+  return (size_t)n * (13 + 1 + 4 + 2 * (size_t)(levels + 1)) + 64;
+}
+
+// C (rows x cols) = A (rows x kd) B (kd x cols), all with leading dimension ld; C = 0 when kd = 0.
+template <typename T>
+static void merge_product(cudaStream_t s, int rows, int cols, int kd, const T *A, const T *B, T *C, int ld) {
+  if (rows <= 0 || cols <= 0) return;
+  if (kd <= 0) {
+    cudaMemset2DAsync(C, (size_t)ld * sizeof(T), 0, (size_t)rows * sizeof(T), (size_t)cols, s);
+    return;
+  }
+  gemm<T>(s, 'N', 'N', rows, cols, kd, T(1), A, ld, B, ld, T(0), C, ld);
 }
 
 template <typename T>
@@ -639,6 +735,7 @@ int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork,
   int *ip = iwork;
   W.perm = ip; ip += n; W.ndpos = ip; ip += n; W.dfpos = ip; ip += n; W.org = ip; ip += n;
   W.srcinfo = ip; ip += n; W.mK = ip; ip += n; W.mRot = ip; ip += n; ip += n;
+  W.grp = ip; ip += n; W.mK1 = ip; ip += n; W.mK2 = ip; ip += n;
   W.rot_cols = ip; ip += 2 * (size_t)n;
   int *dev_meta = ip;  // bounds + per-level merges and position maps (uploaded below)
 
@@ -680,6 +777,8 @@ int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork,
       const int sn = dc_stage_n<T>(L.max_block);
       dc_deflate_kernel<T><<<nm, 256, dc_stage_bytes<T>(sn), s>>>(dm, e, W, sn);
     }
+    dc_group_kernel<T><<<nm, 256, 0, s>>>(dm, W);
+    count_launch();
     dim3 gr(nm, ceil_div(L.max_block, 256));
     dc_rotate_kernel<T><<<gr, 256, 0, s>>>(dm, Qin, ldq, W);
     int warps_blocks = ceil_div((long long)n * 32, 256);
@@ -692,15 +791,21 @@ int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork,
       dc_small_gemm_kernel<T><<<nm, 256, 0, s>>>(dm, W, n);
       count_launch();
     } else {
-      hK.resize(nm);
+      hK.resize(3 * (size_t)nm);
       cudaMemcpyAsync(hK.data(), W.mK, nm * sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(hK.data() + nm, W.mK1, nm * sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(hK.data() + 2 * (size_t)nm, W.mK2, nm * sizeof(int), cudaMemcpyDeviceToHost, s);
       cudaStreamSynchronize(s);
       for (int k = 0; k < nm; ++k) {
         const Merge &mg = L.merges[k];
         if (mg.m == mg.b || hK[k] == 0) continue;
-        int a = mg.a, N = mg.b - mg.a, K = hK[k];
-        gemm<T>(s, 'N', 'N', N, K, K, T(1), W.Gs + a + (size_t)a * n, n, W.U + (size_t)a * n, n, T(0),
-                W.Qtmp + a + (size_t)a * n, n);
+        const int a = mg.a, m = mg.m, b = mg.b, K = hK[k], K1 = hK[nm + k], K2 = hK[2 * (size_t)nm + k];
+        // Qtmp = Gs U, split by rows: the left rows see only the columns supported there (groups
+        // [0, K2)), the right rows only [K1, K); the other columns are zero in those rows
+        merge_product<T>(s, m - a, K, K2, W.Gs + a + (size_t)a * n, W.U + (size_t)a * n,
+                         W.Qtmp + a + (size_t)a * n, n);
+        merge_product<T>(s, b - m, K, K - K1, W.Gs + m + (size_t)(a + K1) * n, W.U + K1 + (size_t)a * n,
+                         W.Qtmp + m + (size_t)a * n, n);
       }
     }
     dim3 grk(nm, ceil_div(L.max_block, 256));
@@ -729,7 +834,7 @@ constexpr int kNoAllocMaxN = 256;
 constexpr int kNoAllocMaxLevels = 8;                   // ceil(log2 256)
 constexpr size_t kNoAllocWork = 9 * 256 + 2 * 256 + 4 * 256 * 256 + 64;      // doubles
 constexpr size_t kNoAllocPlan = 4 * 256 + 2 * 256 * kNoAllocMaxLevels + 64;  // ints
-constexpr size_t kNoAllocIwork = 10 * 256 + kNoAllocPlan + 64;                // ints
+constexpr size_t kNoAllocIwork = 13 * 256 + kNoAllocPlan + 64;                // ints
 constexpr size_t kNoAllocDoubles = kNoAllocWork + (kNoAllocIwork + 1) / 2 + 32;
 
 // ~2.2 MB per device, held by every GPU that loads the library until process exit. Shared by all
@@ -775,6 +880,7 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
   int *status = ip; ip += 32;
   W.perm = ip; ip += n; W.ndpos = ip; ip += n; W.dfpos = ip; ip += n; W.org = ip; ip += n;
   W.srcinfo = ip; ip += n; W.mK = ip; ip += n; W.mRot = ip; ip += n; ip += n;
+  W.grp = ip; ip += n; W.mK1 = ip; ip += n; W.mK2 = ip; ip += n;
   W.rot_cols = ip; ip += 2 * (size_t)n;
   int *meta = ip;
 
@@ -808,6 +914,8 @@ static int stedc_noalloc_impl(cudaStream_t s, int n, double *d, const double *e_
     dc_sort_kernel<double><<<nm, 256, 0, s>>>(dm, d, e, Qin, n, W);
     const int sn = dc_stage_n<double>(max_block);   // max_block <= 256: under the default 48 KB
     dc_deflate_kernel<double><<<nm, 256, dc_stage_bytes<double>(sn), s>>>(dm, e, W, sn);
+    dc_group_kernel<double><<<nm, 256, 0, s>>>(dm, W);
+    count_launch();
     dim3 gr(nm, ceil_div(max_block, 256));
     dc_rotate_kernel<double><<<gr, 256, 0, s>>>(dm, Qin, n, W);
     int wb = ceil_div((long long)n * 32, 256);
