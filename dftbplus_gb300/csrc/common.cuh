@@ -4,6 +4,8 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -64,6 +66,24 @@ extern std::atomic<long long> g_launches;
 inline void count_launch(long long n = 1) { g_launches += n; }
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Raises the dynamic shared-memory limit of kernel fn to `bytes` on the current device. The limit is
+// a per-device property of the function, so it is recorded per (device, kernel): a process with
+// contexts on several GPUs sets it on each of them once.
+inline cudaError_t ensure_dyn_smem(const void *fn, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, int> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(dev, fn);
+  const auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done[key] = bytes;
+  return e;
+}
 
 // Profiling phases (order documented in include/dftbgpu.h, dftbgpu_profile_enable).
 enum Phase : int {

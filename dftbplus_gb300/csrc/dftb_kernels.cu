@@ -789,11 +789,7 @@ void broyden_step(cudaStream_t s, int natom, int it, int mix_it, int min_iter, i
                   double alpha, double omega0, double minw, double maxw, double wfac, BroydenDev b, double *qin,
                   const double *qout, double *scal) {
   size_t smem = sizeof(double) * ((size_t)b.max_iter + (size_t)b.max_iter * b.max_iter);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(broyden_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  ensure_dyn_smem((const void *)broyden_kernel, 200 * 1024);
   broyden_kernel<<<1, 1024, smem, s>>>(natom, it, mix_it, min_iter, max_iter_scc, tol, alpha, omega0, minw, maxw,
                                        wfac, b, qin, qout, scal);
   count_launch();

@@ -1078,11 +1078,7 @@ __global__ void larft_kernel(int nb, const T *G, int ldg, const T *tau, T *Tf, i
 template <typename T>
 static void larft_launch(cudaStream_t s, int nb, const T *G, int ldg, const T *tau, T *Tf, int ldt) {
   constexpr int kSmem = 2 * OB * (OB + 1) * (int)sizeof(T);
-  static const bool attr = [] {
-    cudaFuncSetAttribute(larft_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    return true;
-  }();
-  (void)attr;
+  ensure_dyn_smem((const void *)larft_kernel<T>, kSmem);
   larft_kernel<T><<<1, OB, kSmem, s>>>(nb, G, ldg, tau, Tf, ldt);
   count_launch();
 }

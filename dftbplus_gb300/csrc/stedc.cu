@@ -769,11 +769,7 @@ int stedc(cudaStream_t s, int n, T *d, T *e, T *Q, int ldq, T *work, int *iwork,
     int nm = (int)L.merges.size();
     dc_sort_kernel<T><<<nm, 256, 0, s>>>(dm, d, e, Qin, ldq, W);
     {
-      static bool attr = false;   // per instantiation: the largest staging size, set once
-      if (!attr) {
-        cudaFuncSetAttribute(dc_deflate_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDcStageBytes);
-        attr = true;
-      }
+      ensure_dyn_smem((const void *)dc_deflate_kernel<T>, kDcStageBytes);
       const int sn = dc_stage_n<T>(L.max_block);
       dc_deflate_kernel<T><<<nm, 256, dc_stage_bytes<T>(sn), s>>>(dm, e, W, sn);
     }

@@ -707,11 +707,7 @@ static void sy2sb_lower(cudaStream_t s, int n, T *A, int lda, T *V1, int ldv, T 
   T *tau1 = w + L.tau1, *T1 = w + L.T1, *X1 = w + L.X1, *X = w + L.X, *X2 = w + L.X2, *Gm = w + L.G, *G2 = w + L.G2,
     *M = w + L.M, *split = w + L.split, *part = w + L.part, *top = w + L.top;
   GridBar *bar = reinterpret_cast<GridBar *>(w + L.ints);
-  static int max_smem_set = 0;
-  if (!max_smem_set) {
-    cudaFuncSetAttribute(panel_qr_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    max_smem_set = 1;
-  }
+  ensure_dyn_smem((const void *)panel_qr_kernel<T>, 200 * 1024);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -807,11 +803,9 @@ void twostage_back(cudaStream_t s, int n, int k, T *Z, int ldz, const T *V1, int
     int *prog = ints + 16 + n;   // after the chase's progress words
     cudaMemsetAsync(err, 0, 2 * sizeof(int), s);
     cudaMemsetAsync(prog, 0, sizeof(int) * (size_t)L.ngrp * nstrip, s);
-    static int g_q2 = 0;
-    if (g_q2 == 0) {
-      cudaFuncSetAttribute(q2_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)q2_smem_bytes<T>());
-      g_q2 = coop_ctas<T>((const void *)q2_apply_kernel<T>, kQ2Cols / 2, q2_smem_bytes<T>());
-    }
+    ensure_dyn_smem((const void *)q2_apply_kernel<T>, (int)q2_smem_bytes<T>());
+    static int g_q2 = 0;   // co-resident CTAs (the same on every GB300)
+    if (g_q2 == 0) g_q2 = coop_ctas<T>((const void *)q2_apply_kernel<T>, kQ2Cols / 2, q2_smem_bytes<T>());
     const int G = std::max(1, std::min(g_q2, L.ngrp * nstrip));
     Q2Args<T> qa{n, k, L.kmax, L.ngrp, nstrip, work + L.V2, work + L.T2, Z, ldz, prog, counter, err, status};
     void *args[] = {&qa};
