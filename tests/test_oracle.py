@@ -135,3 +135,20 @@ def test_scc_golden_fixtures_reproduce():
     assert res.n_iter == int(z["n_iter"])
     assert np.allclose([res.energies[k] for k in ENERGY_KEYS], z["energies"], atol=1e-10, rtol=0)
     assert np.allclose(res.q_out_atom, z["q_out_atom"], atol=1e-10, rtol=0)
+
+
+def test_density_idempotent_and_traced_at_low_temperature(water_model):
+    """Internal consistency of the oracle's converged state (no reference data needed): with a gap
+    far above kT every level is filled with 2 or 0 electrons, so rho S rho = 2 rho (spin-unpolarised
+    idempotency in the S metric) and Tr(rho S) = N_el; the eigenvectors are S-orthonormal."""
+    from dftbplus_gb300 import synth
+    c, s = synth.water_cluster(8, 6.3, 11)
+    sys_ = O.System(water_model, c, s)
+    res = O.run_scc(sys_, kt=1e-5)
+    assert res.converged
+    H0, S = O.build_h0_s(sys_)
+    n_el = water_model.n_electrons(sys_.species, 0.0)
+    assert np.all((np.abs(res.filling - 2.0) < 1e-12) | (np.abs(res.filling) < 1e-12))
+    assert abs(np.trace(res.rho @ S) - n_el) < 1e-10
+    assert np.max(np.abs(res.rho @ S @ res.rho - 2.0 * res.rho)) < 1e-10
+    assert np.max(np.abs(res.C.T @ S @ res.C - np.eye(S.shape[0]))) < 1e-10
